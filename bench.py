@@ -1,0 +1,329 @@
+"""Benchmark: LM edges linearised per second of a multi-camera local BA.
+
+Workload (one "step"): a full 10-iteration Levenberg-Marquardt local bundle
+adjustment of the 30-keyframe x 3-camera window with 20k map points
+(~150k observations, 5% outliers, Huber sqrt(5.991), first 2 keyframes fixed),
+solved on one GPU by libmcba.  Metric: active edges x LM iterations / solve
+time.  Seeded synthetic data with the benchmark's shapes and noise model.
+
+  value   device-resident: problem compiled and uploaded once, every step
+          restores the initial estimates on the device and solves (CUDA
+          events inside the library), L2 flushed between steps.
+  e2e     through the C ABI with host buffers: load + optimize (structure
+          compilation, H2D, solve, D2H of the solution) per step.
+  cpu_baseline  the oracle (a restatement of the reference's g2o path), one
+          thread, on a bounded number of whole solves of the same problem.
+
+--impl reference times the oracle with every host thread on the same
+workload (the reference's own code cannot be built here).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+LBA_ITERS = 10
+METRIC = "LM edges linearised/s (local BA, 30 KF x 3 cams, 20k points)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="mcba", choices=["mcba", "reference"])
+    ap.add_argument("--config", type=int, default=2, choices=[1, 2, 5])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(
+        os.environ.get("LOCAL_RANK", "0"))
+
+
+# ------------------------------------------------------------------ clocks --
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for i, n in enumerate(names):
+                if len(r) > 5 + i and r[5 + i].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------- roofline --
+def algorithmic_bytes_linearize(st: dict, precision: str) -> int:
+    """Compulsory bytes of one linearisation launch.
+
+    Per active edge: the streamed record (pose, point, camera, flags,
+    information, Huber threshold, u v) = 28 B in FP32 / 40 B in FP64, plus the
+    6x3 Hpl block it must produce for the Schur step (72 B / 144 B).
+    Per free point: read X (12 B / 24 B) and write Hll + b_l (9 values).
+    Per free pose: read the pose (48 B / 96 B) and write Hpp + b_p (27 values)."""
+    w = 4 if precision == "mixed" else 8
+    rec = 28 if precision == "mixed" else 40
+    E, Lf, Kf = st["n_active_edges"], st["n_free_points"], st["n_free_poses"]
+    return E * (rec + 18 * w) + Lf * (3 * w + 9 * w) + Kf * (12 * w + 27 * w)
+
+
+def read_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def read_traffic(kernel: str):
+    """Per-launch DRAM bytes of `kernel` recorded from an ncu capture in profiles/."""
+    prof = os.path.join(ROOT, "profiles")
+    try:
+        names = sorted(os.listdir(prof))
+    except OSError:
+        return None
+    for n in names:
+        if not n.endswith(".md"):
+            continue
+        with open(os.path.join(prof, n)) as f:
+            for line in f:
+                if line.startswith(f"traffic_bytes_per_launch[{kernel}]:"):
+                    try:
+                        return int(float(line.split(":", 1)[1].strip()))
+                    except ValueError:
+                        return None
+    return None
+
+
+# --------------------------------------------------------------------- arms --
+def cpu_baseline(pr, seconds: float) -> dict:
+    from oracle import oracle
+
+    t0 = time.perf_counter()
+    runs, edges = 0, 0
+    while True:
+        r = oracle.optimize(pr, LBA_ITERS, n_threads=1, log_cap=1)
+        runs += 1
+        edges += r["n_active_edges"] * max(r["iterations_done"], 0)
+        if time.perf_counter() - t0 >= seconds or runs >= 50:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": edges / dt, "unit": "edges/s", "cores": 1, "kind": "port",
+            "sample": f"{runs} whole {LBA_ITERS}-iteration solves of the same problem, serial oracle, {dt:.1f} s"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from mcvslam_gb300 import synth
+    from oracle import oracle
+
+    pr = synth.config(args.config)
+    threads = os.cpu_count() or 1
+    times, edges = [], 0
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        r = oracle.optimize(pr, LBA_ITERS, n_threads=threads, log_cap=1)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(dt)
+            edges = r["n_active_edges"] * max(r["iterations_done"], 0)
+    ms = 1e3 * statistics.mean(times)
+    value = edges / (ms / 1e3)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+        "config": {"workload": pr.name, "edges": pr.n_edges, "keyframes": pr.n_poses, "points": pr.n_points,
+                   "lm_iterations": LBA_ITERS, "solver": "oracle restatement of g2o LM + Schur, OpenMP"},
+        "cpu_baseline": {"value": value, "unit": "edges/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} whole solves after {args.warmup} warm-up"},
+        "e2e": {"value": value, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_mcba(args):
+    import torch
+
+    from mcvslam_gb300 import _native, ba, synth
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+
+        dist_mod.init_process_group("nccl")
+        dist = dist_mod
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    pr = synth.config(args.config)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    # device-resident leg
+    s = ba.Solver(precision=args.precision, device=local, profile=True)
+    s.load(pr)
+    s.prepare()
+    for _ in range(args.warmup):
+        s.solve_prepared(LBA_ITERS)
+    clocks = ClockSampler(local)
+    step_ms, launches, stats = [], 0, []
+    phase_ms = np.zeros(8)
+    phase_n = np.zeros(8, np.int64)
+    barrier()
+    clocks.start()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        st = s.solve_prepared(LBA_ITERS)
+        step_ms.append(st["ms_total"])
+        launches += st["kernel_launches"]
+        phase_ms += np.array(st["ms_phase"])
+        phase_n += np.array(st["n_phase"])
+        stats.append(st)
+    barrier()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    st0 = stats[-1]
+    edges_per_step = st0["edges_linearized"]
+    ms = statistics.mean(step_ms)
+    t_max = ms
+    if dist:
+        tt = torch.tensor([ms], device=f"cuda:{local}")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+    value = world * edges_per_step / (t_max / 1e3)
+
+    # per-phase breakdown and roofline of the linearisation kernel
+    phases = {n: {"ms_total": float(phase_ms[i]), "launches": int(phase_n[i]),
+                  "ms_per_launch": float(phase_ms[i] / phase_n[i]) if phase_n[i] else None}
+              for i, n in enumerate(_native.PHASES)}
+    lin_ms = phase_ms[0] / max(phase_n[0], 1)
+    alg = algorithmic_bytes_linearize(st0, args.precision)
+    peak, peak_kind = read_peaks()
+    achieved = alg / (lin_ms / 1e3) / 1e9
+    roofline = {"kernel": "k_linearize", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind, "traffic": read_traffic("k_linearize"),
+                "algorithmic_bytes_per_launch": alg, "ms_per_launch": lin_ms}
+
+    # end-to-end leg through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        e2e_ms, h2d, d2h = [], 0, 0
+        for i in range(args.warmup + args.steps):
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            with ba.Solver(precision=args.precision, device=local) as s2:
+                s2.load(pr)
+                st2 = s2.optimize(LBA_ITERS)
+                qt, X = s2.state()
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t1
+            if i >= args.warmup:
+                e2e_ms.append(1e3 * dt)
+                h2d, d2h = st2["h2d_bytes"], st2["d2h_bytes"]
+        e2e = {"value": world * st2["edges_linearized"] / (statistics.mean(e2e_ms) / 1e3), "unit": "edges/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "ms_per_step": statistics.mean(e2e_ms)}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(pr, args.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64",
+            "data": "synthetic (seeded generator with the benchmark's shapes and noise model)",
+            "config": {"workload": pr.name, "edges": pr.n_edges, "active_edges": st0["n_active_edges"],
+                       "keyframes": pr.n_poses, "free_keyframes": st0["n_free_poses"], "points": pr.n_points,
+                       "lm_iterations": LBA_ITERS, "precision": args.precision,
+                       "l2": "flushed (256 MB write) before every step; working set ~30 MB < L2",
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "ba_solve_ms": ms, "final_chi2": st0["final_chi2"], "lm_trials": st0["trials"]},
+            "e2e": e2e, "cpu_baseline": cpu, "roofline": roofline, "phases": phases,
+            "clocks": clk, "gpu_launches": int(launches), "wall_s_timed_region": wall,
+        }
+        print(json.dumps(line), flush=True)
+    s.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_mcba(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,286 @@
+/*
+ * mcba.h -- C ABI of the GB300 bundle-adjustment solver (libmcba.so).
+ *
+ * Drop-in replacement for MCVSLAM's BAoptimizer (include/BAoptimizer.hpp:29-80,
+ * src/BAoptimizer.cpp:13-143 of the reference) and for the two PoseEstimation
+ * drivers built on it (include/PoseEstimation.hpp:35-119,
+ * src/PoseEstimation.cpp:48-151).  Every entry point takes plain pointers and
+ * sizes, returns an int status (MCBA_OK == 0) and never throws.  A problem
+ * handle is used by one host thread at a time; distinct handles are
+ * independent.  All numeric inputs cross the boundary in the precision the
+ * reference hands to g2o (float poses, points, pixels, information and Huber
+ * thresholds) and the solver keeps its state in FP64 internally.
+ */
+#ifndef MCBA_H
+#define MCBA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCBA_ABI_VERSION 1
+
+/* ------------------------------------------------------------ status -- */
+enum {
+  MCBA_OK = 0,
+  MCBA_ERR_INVALID = 1,     /* bad argument: unknown id, NULL pointer, bad size */
+  MCBA_ERR_EMPTY = 2,       /* nothing to optimise (g2o: "0 vertices to optimize") */
+  MCBA_ERR_NOT_PD = 3,      /* reduced camera system not positive definite */
+  MCBA_ERR_NONFINITE = 4,   /* NaN/Inf in the inputs */
+  MCBA_ERR_TIMEOUT = 5,     /* a bounded device wait gave up */
+  MCBA_ERR_CUDA = 6,        /* CUDA runtime error (see mcba_last_error) */
+  MCBA_ERR_NOMEM = 7,       /* device or host allocation failed */
+  MCBA_ERR_NO_DEVICE = 8,   /* no CUDA device */
+  MCBA_ERR_TOO_LARGE = 9    /* request above a documented maximum */
+};
+
+/* Edge kinds of include/OptimizeTypes.hpp */
+enum {
+  MCBA_EDGE_MONO = 0,   /* EdgeSE3XYZ2Camera: point -> body pose through T_cam_body (hpp:70-117) */
+  MCBA_EDGE_STEREO = 1, /* EdgeStereoSE3ProjectXYZ: (u, v, u_right), pose used as T_cam_world (hpp:119-157) */
+  MCBA_EDGE_UNARY = 2   /* EdgeSE3XYZ2CameraOnlyPose: constant world point (hpp:20-68) */
+};
+
+enum {
+  MCBA_PREC_FP64 = 0,  /* plain: every step in FP64 (matches g2o) */
+  MCBA_PREC_MIXED = 1  /* FP32 residuals/Jacobians/Schur blocks, FP64 Cholesky, LM test and retraction */
+};
+
+typedef struct mcba_problem mcba_problem;
+
+typedef struct mcba_options {
+  int32_t precision;   /* MCBA_PREC_* */
+  int32_t device;      /* CUDA device ordinal */
+  double tau;          /* LM initial damping factor, g2o default 1e-5 (optimization_algorithm_levenberg.cpp:43) */
+  int32_t max_trials;  /* maxTrialsAfterFailure, default 10 (optimization_algorithm_levenberg.cpp:50) */
+  int32_t use_graph;   /* 1: run the LM loop as one CUDA graph with device-side control */
+  int32_t profile;     /* 1: time every phase with CUDA events (mcba_stats.ms_phase) */
+  void* stream;        /* cudaStream_t to run on, NULL for a library-owned stream */
+} mcba_options;
+
+/* Phases timed when mcba_options.profile is set, named after g2o's
+ * G2OBatchStatistics fields (core/batch_stats.h:40-76). */
+enum {
+  MCBA_PHASE_LINEARIZE = 0,   /* timeQuadraticForm: per-edge residual/Jacobian/quadratic terms */
+  MCBA_PHASE_REDUCE = 1,      /* Hpp / Hll / b segmented sums (+ lambda init) */
+  MCBA_PHASE_SCHUR_EDGE = 2,  /* timeSchurComplement: Y = Hpl Dinv per edge */
+  MCBA_PHASE_SCHUR_PAIRS = 3, /* timeSchurComplement: reduced-camera block products */
+  MCBA_PHASE_SCHUR_ASSEMBLE = 4, /* dense reduced camera matrix + b_schur */
+  MCBA_PHASE_CHOLESKY = 5,    /* timeLinearSolver: FP64 factorisation and solves */
+  MCBA_PHASE_UPDATE = 6,      /* timeUpdate: back-substitution, retraction */
+  MCBA_PHASE_COST = 7,        /* timeResiduals: activeRobustChi2 + LM decision */
+  MCBA_NUM_PHASES = 8
+};
+
+typedef struct mcba_stats {
+  int32_t iterations;        /* g2o optimize() return value */
+  int32_t trials;            /* LM trials run (linear solves) */
+  int32_t n_active_edges;
+  int32_t n_free_poses;
+  int32_t n_free_points;
+  int32_t status;            /* MCBA_* of the last solve */
+  double initial_chi2;       /* activeRobustChi2 before the first iteration */
+  double final_chi2;         /* activeRobustChi2 at the returned state */
+  double lambda;             /* damping after the last trial */
+  int64_t edges_linearized;  /* active edges x iterations */
+  double ms_total;           /* device time of the whole solve (CUDA events) */
+  double ms_linearize;       /* device time of the linearisation phases */
+  double ms_host_prepare;    /* host time of structure compilation and upload */
+  double ms_phase[MCBA_NUM_PHASES];   /* device time per phase (profile option) */
+  int32_t n_phase[MCBA_NUM_PHASES];   /* timed launches per phase */
+  int64_t kernel_launches;   /* device kernels launched by the solve */
+  int64_t h2d_bytes;         /* host-to-device bytes copied by the call */
+  int64_t d2h_bytes;         /* device-to-host bytes copied by the call */
+} mcba_stats;
+
+typedef struct mcba_trial_log {
+  int32_t iteration;
+  int32_t trial;
+  double chi_before;
+  double chi_after;
+  double lambda;
+  double scale;
+  double rho;
+  int32_t accepted;
+  int32_t solve_ok;
+} mcba_trial_log;
+
+/* ------------------------------------------------------- life cycle -- */
+int mcba_abi_version(void);
+const char* mcba_status_string(int status);
+void mcba_default_options(mcba_options* opt);
+int mcba_device_count(int* count);
+
+/* Replaces BAoptimizer::BAoptimizer (src/BAoptimizer.cpp:13-18). */
+int mcba_create(const mcba_options* opt, mcba_problem** out);
+/* Replaces BAoptimizer::~BAoptimizer; frees every host and device buffer. */
+int mcba_destroy(mcba_problem* p);
+/* Message of the last error on this handle ("" when none). */
+const char* mcba_last_error(const mcba_problem* p);
+/* Drops every vertex and edge, keeps the options and device buffers. */
+int mcba_clear(mcba_problem* p);
+
+/* ------------------------------------------------------- graph build -- */
+/* Camera model Pinhole (modules/camera/Pinhole.cpp:55-60,105-116): K = fx fy cx
+ * cy, bf for stereo edges, T_cam_body row-major float 4x4 (the Tcb argument of
+ * EdgeSE3XYZ2Camera, include/OptimizeTypes.hpp:74, converted as
+ * Converter::toSE3Quat, src/Converter.cc:31-39). */
+int mcba_add_camera(mcba_problem* p, const float K[4], float bf, const float T_cam_body[16], int32_t* id);
+
+/* BAoptimizer::addKeyFrame (src/BAoptimizer.cpp:22-31): T_body_world as a
+ * row-major float 4x4; fixed as in setFixed.  (The reference also fixes the
+ * keyframe with id 0; callers pass that as fixed.) */
+int mcba_add_keyframe(mcba_problem* p, const float T_body_world[16], int fixed, int32_t* id);
+/* Same with the estimate given as FP64 quaternion (x y z w) + translation. */
+int mcba_add_keyframe_qt(mcba_problem* p, const double qt[7], int fixed, int32_t* id);
+
+/* BAoptimizer::addMapppint (src/BAoptimizer.cpp:33-42): marginalised point. */
+int mcba_add_mappoint(mcba_problem* p, const float Xw[3], int fixed, int32_t* id);
+
+/* BAoptimizer::addEdge / addEdgeToBody (src/BAoptimizer.cpp:45-65,90-108):
+ * EdgeSE3XYZ2Camera with the camera's T_cam_body, information
+ * inv_sigma2 * I, Huber kernel of threshold huber_delta (<= 0: no kernel). */
+int mcba_add_edge_mono(mcba_problem* p, int32_t keyframe, int32_t mappoint, int32_t camera, float u,
+                       float v, float inv_sigma2, float huber_delta, int32_t* id);
+/* BAoptimizer::addEdgeStereo (src/BAoptimizer.cpp:67-88). */
+int mcba_add_edge_stereo(mcba_problem* p, int32_t keyframe, int32_t mappoint, int32_t camera, float u,
+                         float v, float u_right, float inv_sigma2, float huber_delta, int32_t* id);
+/* EdgeSE3XYZ2CameraOnlyPose (include/OptimizeTypes.hpp:20-68): unary edge on a
+ * keyframe with a constant world point. */
+int mcba_add_edge_posonly(mcba_problem* p, int32_t keyframe, int32_t camera, const float Xw[3], float u,
+                          float v, float inv_sigma2, float huber_delta, int32_t* id);
+
+/* Bulk form of the three edge calls: type[n] (MCBA_EDGE_*), obs[n][3]
+ * (u, v, u_right), Xw[n][3] only read for unary edges (may be NULL when there
+ * are none).  Ids are consecutive from *first_id. */
+int mcba_add_edges(mcba_problem* p, int32_t n, const uint8_t* type, const int32_t* keyframe,
+                   const int32_t* mappoint, const int32_t* camera, const float* obs, const float* Xw,
+                   const float* inv_sigma2, const float* huber_delta, int32_t* first_id);
+
+/* Whole-problem bulk loader in the layout of the synthetic generator:
+ * cameras, keyframes (float 4x4), points, edges (unary edges take their
+ * constant point from point_Xw[edge_point]).  Equivalent to the add_* calls
+ * in array order. */
+typedef struct mcba_problem_desc {
+  int32_t n_cams;
+  const float* cam_K;     /* [n_cams][4] */
+  const float* cam_bf;    /* [n_cams] */
+  const float* cam_Tcb;   /* [n_cams][16] */
+  int32_t n_poses;
+  const float* pose_Tcw;  /* [n_poses][16] */
+  const uint8_t* pose_fixed;
+  int32_t n_points;
+  const float* point_Xw;  /* [n_points][3] */
+  const uint8_t* point_fixed;
+  int32_t n_edges;
+  const uint8_t* edge_type;
+  const int32_t* edge_pose;
+  const int32_t* edge_point;
+  const int32_t* edge_cam;
+  const float* edge_obs;  /* [n_edges][3] */
+  const float* edge_info;
+  const float* edge_delta;
+  const uint8_t* edge_robust; /* may be NULL: all robust */
+  const uint8_t* edge_level;  /* may be NULL: all level 0 */
+} mcba_problem_desc;
+int mcba_load(mcba_problem* p, const mcba_problem_desc* d);
+
+/* BAoptimizer::getEdgeSize (include/BAoptimizer.hpp:43). */
+int mcba_edge_count(const mcba_problem* p, int32_t* n);
+int mcba_vertex_count(const mcba_problem* p, int32_t* n_keyframes, int32_t* n_mappoints);
+
+/* ------------------------------------------------------------ solve -- */
+/* BAoptimizer::optimize(n) (src/BAoptimizer.cpp:110-114): initializeOptimization
+ * on level-0 edges, then n Levenberg-Marquardt iterations with g2o's damping
+ * rules.  stats may be NULL. */
+int mcba_optimize(mcba_problem* p, int32_t iterations, mcba_stats* stats);
+
+/* Device-resident re-solve, for timing with the inputs already in device
+ * memory: mcba_prepare compiles and uploads the problem once (and keeps a
+ * device copy of the initial estimates); every mcba_solve_prepared restores
+ * that initial state on the device and runs the LM iterations without any
+ * host<->device copy of problem data.  The result stays on the device until
+ * mcba_fetch_state copies it back into the handle (mcba_get_* then read it). */
+int mcba_prepare(mcba_problem* p);
+int mcba_solve_prepared(mcba_problem* p, int32_t iterations, mcba_stats* stats);
+int mcba_fetch_state(mcba_problem* p);
+
+/* Per-trial record of the last optimize (iteration, trial, chi2 before/after,
+ * lambda, scale, rho, accepted, solve_ok). */
+int mcba_trial_log_get(const mcba_problem* p, mcba_trial_log* out, int32_t cap, int32_t* n);
+
+/* ----------------------------------------------------- edge control -- */
+/* e->computeError(); e->chi2() for every edge at the current estimate (the
+ * input of the filter callbacks, src/PoseEstimation.cpp:98-116,132-151). */
+int mcba_edge_chi2(mcba_problem* p, double* chi2);
+/* e->setLevel / e->level(): 0 = optimised, 1 = excluded. */
+int mcba_set_edge_levels(mcba_problem* p, const uint8_t* levels);
+int mcba_get_edge_levels(const mcba_problem* p, uint8_t* levels);
+/* e->setRobustKernel(0) when robust[i] == 0, restores the Huber kernel otherwise. */
+int mcba_set_edge_robust(mcba_problem* p, const uint8_t* robust);
+
+/* ---------------------------------------------------------- read back -- */
+/* BAoptimizer::eval(KeyFrame) (src/BAoptimizer.cpp:121-126): float 4x4
+ * T_body_world as Converter::toCvMat (src/Converter.cc:41-52). */
+int mcba_get_keyframe(const mcba_problem* p, int32_t id, float T_body_world[16]);
+int mcba_get_keyframe_qt(const mcba_problem* p, int32_t id, double qt[7]);
+/* BAoptimizer::eval(MapPointRef) (src/BAoptimizer.cpp:128-132). */
+int mcba_get_mappoint(const mcba_problem* p, int32_t id, float Xw[3]);
+/* Bulk FP64 state: qt[n_keyframes][7], X[n_mappoints][3] (either may be NULL). */
+int mcba_get_state(const mcba_problem* p, double* qt, double* X);
+/* Overwrites the FP64 estimates (warm start; quaternions are renormalised
+ * with w >= 0 as SE3Quat does).  Either pointer may be NULL. */
+int mcba_set_state(mcba_problem* p, const double* qt, const double* X);
+
+/* BAoptimizer::DumpCalculationGraph (src/BAoptimizer.cpp:116-119): writes the
+ * pose Hessian Hpp of the last linearisation as upper-triangular Octave text. */
+int mcba_dump_hessian(mcba_problem* p, const char* path);
+
+/* ------------------------------------------------------------ drivers -- */
+/* PoseEstimation::PoseOptimization (src/PoseEstimation.cpp:48-130) on a
+ * problem holding one free keyframe and fixed points: `rounds` optimisations
+ * of `iterations` each, edges with chi2 >= chi2_threshold set to level 1 after
+ * each round, robust kernels dropped after round `drop_robust_round`, early
+ * stop when fewer than 10 edges remain.  *inliers = nInitial - nBad (0 with
+ * fewer than 3 edges); *pose_written = whether the reference would call
+ * SetPose.  Edge levels are left as the filter set them. */
+int mcba_pose_optimization(mcba_problem* p, int32_t rounds, int32_t iterations, float chi2_threshold,
+                           int32_t drop_robust_round, int32_t* inliers, int32_t* pose_written);
+
+/* PoseEstimation::BoundleAdjustment (include/PoseEstimation.hpp:36-119):
+ * optimize(iterations), then FilterCallBack_Chi2 on every level-0 edge
+ * (chi2 >= chi2_threshold -> level 1).  *success_edges reproduces the
+ * reference's return value (the edge count: nBad is never incremented there);
+ * *written = whether recovery_all would run (success_edges > 10). */
+int mcba_local_ba(mcba_problem* p, int32_t iterations, float chi2_threshold, int32_t* success_edges,
+                  int32_t* written);
+
+/* -------------------------------------------- reprojection primitives -- */
+/* Device-pointer entry points behind the autograd harness (no host copies;
+ * all pointers are device memory, stream is a cudaStream_t or NULL).  They
+ * expose EdgeSE3XYZ2Camera's computeError / linearizeOplus
+ * (include/OptimizeTypes.hpp:80-113) plus the rig-extrinsic Jacobian.
+ * Forward: residual r = obs - pi(T_cb * T_bw * X) of n mono edges, with
+ *   pose_qt [n][7] (T_body_world), ext_qt [n][7] (T_cam_body), X [n][3],
+ *   K [n][4], obs [n][2]  ->  res [n][2].  pose_delta / ext_delta [n][6]
+ *   (may be NULL) are applied first as T <- exp(delta) * T.
+ * Backward: given grad_res [n][2], writes the vector-Jacobian products on the
+ *   left-perturbation tangent spaces: g_pose [n][6], g_ext [n][6], g_X [n][3]
+ *   (g2o ordering: rotation first).  Jacobians J_pose [n][2][6],
+ *   J_ext [n][2][6], J_X [n][2][3] are written when the pointers are non-NULL.
+ * double_precision selects FP64 (1) or FP32 (0) buffers. */
+int mcba_reproj_forward(int32_t double_precision, int64_t n, const void* pose_qt, const void* ext_qt,
+                        const void* pose_delta, const void* ext_delta, const void* X, const void* K,
+                        const void* obs, void* res, void* stream);
+int mcba_reproj_backward(int32_t double_precision, int64_t n, const void* pose_qt, const void* ext_qt,
+                         const void* pose_delta, const void* ext_delta, const void* X, const void* K,
+                         const void* grad_res, void* g_pose, void* g_ext, void* g_X, void* J_pose,
+                         void* J_ext, void* J_X, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MCBA_H */

@@ -1,0 +1,158 @@
+"""ctypes binding of libmcba.so (the C ABI in include/mcba.h).
+
+The library is the only compute path: if it is missing or cannot be loaded
+this module raises instead of falling back to anything else.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libmcba.so")
+
+c_float_p = ctypes.POINTER(ctypes.c_float)
+c_double_p = ctypes.POINTER(ctypes.c_double)
+c_u8_p = ctypes.POINTER(ctypes.c_uint8)
+c_i32_p = ctypes.POINTER(ctypes.c_int32)
+
+MCBA_OK = 0
+STATUS = {0: "ok", 1: "invalid argument", 2: "nothing to optimise", 3: "not positive definite",
+          4: "non-finite input", 5: "timeout", 6: "CUDA error", 7: "out of memory", 8: "no CUDA device",
+          9: "too large"}
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int32), ("device", ctypes.c_int32), ("tau", ctypes.c_double),
+                ("max_trials", ctypes.c_int32), ("use_graph", ctypes.c_int32), ("profile", ctypes.c_int32),
+                ("stream", ctypes.c_void_p)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int32), ("trials", ctypes.c_int32), ("n_active_edges", ctypes.c_int32),
+                ("n_free_poses", ctypes.c_int32), ("n_free_points", ctypes.c_int32), ("status", ctypes.c_int32),
+                ("initial_chi2", ctypes.c_double), ("final_chi2", ctypes.c_double), ("lambda_", ctypes.c_double),
+                ("edges_linearized", ctypes.c_int64), ("ms_total", ctypes.c_double),
+                ("ms_linearize", ctypes.c_double), ("ms_host_prepare", ctypes.c_double),
+                ("ms_phase", ctypes.c_double * 8), ("n_phase", ctypes.c_int32 * 8),
+                ("kernel_launches", ctypes.c_int64), ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64)]
+
+    def as_dict(self) -> dict:
+        d = {f: getattr(self, f) for f, _ in self._fields_}
+        d["lambda"] = d.pop("lambda_")
+        d["ms_phase"] = list(d["ms_phase"])
+        d["n_phase"] = list(d["n_phase"])
+        return d
+
+
+PHASES = ["linearize", "reduce", "schur_edge", "schur_pairs", "schur_assemble", "cholesky", "update", "cost"]
+
+
+class TrialLog(ctypes.Structure):
+    _fields_ = [("iteration", ctypes.c_int32), ("trial", ctypes.c_int32), ("chi_before", ctypes.c_double),
+                ("chi_after", ctypes.c_double), ("lambda_", ctypes.c_double), ("scale", ctypes.c_double),
+                ("rho", ctypes.c_double), ("accepted", ctypes.c_int32), ("solve_ok", ctypes.c_int32)]
+
+
+class ProblemDesc(ctypes.Structure):
+    _fields_ = [
+        ("n_cams", ctypes.c_int32), ("cam_K", c_float_p), ("cam_bf", c_float_p), ("cam_Tcb", c_float_p),
+        ("n_poses", ctypes.c_int32), ("pose_Tcw", c_float_p), ("pose_fixed", c_u8_p),
+        ("n_points", ctypes.c_int32), ("point_Xw", c_float_p), ("point_fixed", c_u8_p),
+        ("n_edges", ctypes.c_int32), ("edge_type", c_u8_p), ("edge_pose", c_i32_p),
+        ("edge_point", c_i32_p), ("edge_cam", c_i32_p), ("edge_obs", c_float_p),
+        ("edge_info", c_float_p), ("edge_delta", c_float_p), ("edge_robust", c_u8_p),
+        ("edge_level", c_u8_p),
+    ]
+
+
+_LIB = None
+
+
+def _declare(L):
+    P = ctypes.c_void_p
+    i32 = ctypes.c_int32
+    sig = {
+        "mcba_abi_version": ([], ctypes.c_int),
+        "mcba_status_string": ([ctypes.c_int], ctypes.c_char_p),
+        "mcba_default_options": ([ctypes.POINTER(Options)], None),
+        "mcba_device_count": ([ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+        "mcba_create": ([ctypes.POINTER(Options), ctypes.POINTER(P)], ctypes.c_int),
+        "mcba_destroy": ([P], ctypes.c_int),
+        "mcba_last_error": ([P], ctypes.c_char_p),
+        "mcba_clear": ([P], ctypes.c_int),
+        "mcba_add_camera": ([P, c_float_p, ctypes.c_float, c_float_p, c_i32_p], ctypes.c_int),
+        "mcba_add_keyframe": ([P, c_float_p, ctypes.c_int, c_i32_p], ctypes.c_int),
+        "mcba_add_keyframe_qt": ([P, c_double_p, ctypes.c_int, c_i32_p], ctypes.c_int),
+        "mcba_add_mappoint": ([P, c_float_p, ctypes.c_int, c_i32_p], ctypes.c_int),
+        "mcba_add_edge_mono": ([P, i32, i32, i32, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                c_i32_p], ctypes.c_int),
+        "mcba_add_edge_stereo": ([P, i32, i32, i32, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                  ctypes.c_float, c_i32_p], ctypes.c_int),
+        "mcba_add_edge_posonly": ([P, i32, i32, c_float_p, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                   ctypes.c_float, c_i32_p], ctypes.c_int),
+        "mcba_add_edges": ([P, i32, c_u8_p, c_i32_p, c_i32_p, c_i32_p, c_float_p, c_float_p, c_float_p, c_float_p,
+                            c_i32_p], ctypes.c_int),
+        "mcba_load": ([P, ctypes.POINTER(ProblemDesc)], ctypes.c_int),
+        "mcba_edge_count": ([P, c_i32_p], ctypes.c_int),
+        "mcba_vertex_count": ([P, c_i32_p, c_i32_p], ctypes.c_int),
+        "mcba_optimize": ([P, i32, ctypes.POINTER(Stats)], ctypes.c_int),
+        "mcba_prepare": ([P], ctypes.c_int),
+        "mcba_solve_prepared": ([P, i32, ctypes.POINTER(Stats)], ctypes.c_int),
+        "mcba_fetch_state": ([P], ctypes.c_int),
+        "mcba_trial_log_get": ([P, ctypes.POINTER(TrialLog), i32, c_i32_p], ctypes.c_int),
+        "mcba_edge_chi2": ([P, c_double_p], ctypes.c_int),
+        "mcba_set_edge_levels": ([P, c_u8_p], ctypes.c_int),
+        "mcba_get_edge_levels": ([P, c_u8_p], ctypes.c_int),
+        "mcba_set_edge_robust": ([P, c_u8_p], ctypes.c_int),
+        "mcba_get_keyframe": ([P, i32, c_float_p], ctypes.c_int),
+        "mcba_get_keyframe_qt": ([P, i32, c_double_p], ctypes.c_int),
+        "mcba_get_mappoint": ([P, i32, c_float_p], ctypes.c_int),
+        "mcba_get_state": ([P, c_double_p, c_double_p], ctypes.c_int),
+        "mcba_set_state": ([P, c_double_p, c_double_p], ctypes.c_int),
+        "mcba_dump_hessian": ([P, ctypes.c_char_p], ctypes.c_int),
+        "mcba_pose_optimization": ([P, i32, i32, ctypes.c_float, i32, c_i32_p, c_i32_p], ctypes.c_int),
+        "mcba_local_ba": ([P, i32, ctypes.c_float, c_i32_p, c_i32_p], ctypes.c_int),
+        "mcba_reproj_forward": ([i32, ctypes.c_int64, P, P, P, P, P, P, P, P, P], ctypes.c_int),
+        "mcba_reproj_backward": ([i32, ctypes.c_int64, P, P, P, P, P, P, P, P, P, P, P, P, P, P], ctypes.c_int),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    return L
+
+
+def lib(build_if_missing: bool = True):
+    """Load libmcba.so (building it first when it is missing or stale)."""
+    global _LIB
+    if _LIB is None:
+        if build_if_missing:
+            from mcvslam_gb300 import build as _build
+            _build.build()
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"libmcba.so not found at {LIB_PATH}; build it with mcvslam_gb300.build.build()")
+        _LIB = _declare(ctypes.CDLL(LIB_PATH))
+    return _LIB
+
+
+class MCBAError(RuntimeError):
+    def __init__(self, status: int, msg: str = ""):
+        super().__init__(f"mcba status {status} ({STATUS.get(status, '?')}){': ' + msg if msg else ''}")
+        self.status = status
+
+
+def check(status: int, handle=None) -> int:
+    if status != MCBA_OK:
+        msg = ""
+        if handle:
+            m = lib().mcba_last_error(handle)
+            msg = m.decode() if m else ""
+        raise MCBAError(status, msg)
+    return status
+
+
+def device_count() -> int:
+    n = ctypes.c_int(0)
+    lib().mcba_device_count(ctypes.byref(n))
+    return n.value

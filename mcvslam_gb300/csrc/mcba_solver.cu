@@ -1,0 +1,1446 @@
+// mcba_solver.cu -- GB300 Levenberg-Marquardt bundle-adjustment solver.
+//
+// One LM solve of MCVSLAM's BAoptimizer (g2o OptimizationAlgorithmLevenberg
+// over BlockSolver<6,3> with Schur elimination of the points) as device
+// kernels:
+//   linearize      per-edge residual, Huber weight, Jacobians and quadratic
+//                  form terms (base_binary_edge.hpp:64-136); pose terms
+//                  reduced per CTA (one pose per CTA), point terms and Hpl
+//                  written per edge in point-sorted order
+//   pose/point reduce  deterministic segmented sums into Hpp, Hll, b
+//   schur_edge     per edge Y = Hpl Dinv and q = Hpl Dinv b_l
+//                  (block_solver.hpp:346-374)
+//   schur_pairs    reduced camera blocks S_ab -= sum Y_i Hpl_j^T over the
+//                  edge pairs of every block (block_solver.hpp:376-391),
+//                  one warp per pair chunk, no atomics
+//   chol_*         blocked FP64 Cholesky of the reduced camera system with
+//                  b_schur as an extra row (forward substitution for free)
+//   backsolve / backsub / update   x_p, x_l = Dinv(b_l - Hpl^T x_p), the SE3
+//                  exp retraction and the point update, both into the other
+//                  half of a double-buffered state (push/pop become a flip)
+//   cost / decide  activeRobustChi2 and g2o's accept/reject, lambda and nu
+//                  update (optimization_algorithm_levenberg.cpp:92-141) on
+//                  the device.
+// The linearisation real type R is double (plain) or float (mixed); the
+// Cholesky, damping, gain ratio and retraction are FP64 in both.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mcba_device.cuh"
+#include "mcba_internal.h"
+
+namespace mcba {
+using namespace dev;
+
+namespace {
+
+constexpr int kRow = 28;   // per canonical edge: Hpl 6x3 | Hll upper 6 | b_l 3 | pad
+constexpr int kYQ = 24;    // per canonical edge: Y 6x3 | q 6
+constexpr int kNB = 32;    // Cholesky tile
+constexpr int kLinThreads = 256;
+
+// upper-triangle slot of a 6x6 entry (i <= j)
+__host__ __device__ constexpr int u6(int i, int j) { return i * 6 - (i * (i - 1)) / 2 + (j - i); }
+__host__ __device__ constexpr int u3(int i, int j) { return i * 3 - (i * (i - 1)) / 2 + (j - i); }
+
+struct LMState {
+  double lambda, ni, current_chi, temp_chi, rho, scale, initial_chi;
+  int iteration, trial, cur, solve_ok;
+  int trial_continue, terminate, total_trials, n_log;
+  int max_trials, max_log, last_accepted, pad;
+};
+
+struct Bufs {
+  // state (ping-pong)
+  double* pose_qt[2];  // [K][8]
+  PoseLinD* pd[2];
+  PoseLinF* pf[2];
+  double* Xd[2];       // [P+U][3]
+  float4* Xf[2];
+  CamD* cd;
+  CamF* cf;
+  // structure
+  EdgeRec* recs;
+  float* obs;
+  int* chunk_begin;
+  int* chunk_pose;
+  int* pose_chunk_begin;
+  int* pt_begin;
+  int* canon_pose_h;
+  int* canon_point_h;
+  int2* pairs;
+  int* pchunk_begin;
+  int* block_ab;
+  int* block_chunk_begin;
+  int* pose_canon_begin;
+  int* pose_canon_list;
+  int* free_pose_ids;
+  int* free_point_ids;
+  // numeric workspaces (R-typed, stored as bytes)
+  void* rows;       // [Ec][kRow]
+  void* partials;   // [nchunk][32]
+  void* Hpp;        // [Kf][36]
+  void* Hll;        // [Lf][6]
+  void* b;          // [6Kf + 3Lf]
+  void* yq;         // [Ec][kYQ]
+  void* ppart;      // [npchunk][36]
+  double* S;        // [(ld+32) x ld]
+  double* x;        // [6Kf + 3Lf]
+  double* cost_part;
+  double* scale_part;
+  LMState* lm;
+  mcba_trial_log* log;
+};
+
+template <typename R>
+struct Ptrs {
+  __host__ __device__ static R* p(void* v) { return reinterpret_cast<R*>(v); }
+};
+
+__device__ __forceinline__ StateView make_view(const Bufs& B, int which) {
+  StateView v;
+  v.pd = B.pd[which];
+  v.pf = B.pf[which];
+  v.Xd = B.Xd[which];
+  v.Xf = B.Xf[which];
+  v.cd = B.cd;
+  v.cf = B.cf;
+  return v;
+}
+
+// ------------------------------------------------------------ kernels --
+__global__ void k_pose_lin(const double* __restrict__ qt, int n, PoseLinD* pd, PoseLinF* pf) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* q = qt + 8 * (size_t)i;
+  double Rm[9];
+  quat_to_R(q, Rm);
+  PoseLinD d;
+  PoseLinF f;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    d.R[k] = Rm[k];
+    f.R[k] = (float)Rm[k];
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) d.t[k] = q[4 + k];
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    f.c[k] = (float)(-(Rm[k] * q[4] + Rm[3 + k] * q[5] + Rm[6 + k] * q[6]));
+  pd[i] = d;
+  pf[i] = f;
+}
+
+__global__ void k_points_f(const double* __restrict__ X, int n, float4* Xf) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  Xf[i] = make_float4((float)X[3 * (size_t)i], (float)X[3 * (size_t)i + 1], (float)X[3 * (size_t)i + 2], 0.f);
+}
+
+// Per-edge linearisation (buildSystem's edge loop, block_solver.hpp:490-506).
+template <typename R>
+__global__ void __launch_bounds__(kLinThreads) k_linearize(Bufs B) {
+  const int c = blockIdx.x;
+  const int jb = B.chunk_begin[c], je = B.chunk_begin[c + 1];
+  const int ph = B.chunk_pose[c];
+  const int j = jb + threadIdx.x;
+  const StateView v = make_view(B, B.lm->cur);
+  R acc[32];
+#pragma unroll
+  for (int k = 0; k < 32; ++k) acc[k] = R(0);
+  if (j < je) {
+    const EdgeRec r = B.recs[j];
+    const float obs[3] = {B.obs[3 * (size_t)j], B.obs[3 * (size_t)j + 1], B.obs[3 * (size_t)j + 2]};
+    R Pb[3], Pc[3], e[3], chi2;
+    transform(r, v, Pb, Pc);
+    edge_error<R>(r, obs, v, Pc, e, chi2);
+    const R info = (R)r.info;
+    R s = R(1);
+    if (r.robust) s = huber_d1<R>(chi2, (R)r.delta);
+    const R w = s * info;
+    R Jl[3][3], Jp[3][6];
+    edge_jac<R>(r, v, Pb, Pc, Jl, Jp);
+    R om[3];
+    const bool d3 = r.dim == 3;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) om[k] = (k < 2 || d3) ? -(info * e[k]) * s : R(0);
+    R wJp[3][6];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int i = 0; i < 6; ++i) wJp[k][i] = (k < 2 || d3) ? Jp[k][i] * w : R(0);
+    if (r.point_h >= 0) {
+      R* row = Ptrs<R>::p(B.rows) + (size_t)r.canon * kRow;
+      R out[kRow];
+#pragma unroll
+      for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          R h = R(0);
+          if (r.pose_h >= 0) {
+            h = wJp[0][i] * Jl[0][q] + wJp[1][i] * Jl[1][q];
+            if (d3) h += wJp[2][i] * Jl[2][q];
+          }
+          out[i * 3 + q] = h;
+        }
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+#pragma unroll
+        for (int q = i; q < 3; ++q) {
+          R h = (Jl[0][i] * w) * Jl[0][q] + (Jl[1][i] * w) * Jl[1][q];
+          if (d3) h += (Jl[2][i] * w) * Jl[2][q];
+          out[18 + u3(i, q)] = h;
+        }
+        R bb = Jl[0][i] * om[0] + Jl[1][i] * om[1];
+        if (d3) bb += Jl[2][i] * om[2];
+        out[24 + i] = bb;
+      }
+      out[27] = R(0);
+#pragma unroll
+      for (int k = 0; k < kRow; ++k) row[k] = out[k];
+    }
+    if (r.pose_h >= 0) {
+#pragma unroll
+      for (int i = 0; i < 6; ++i) {
+#pragma unroll
+        for (int q = i; q < 6; ++q) {
+          R h = wJp[0][i] * Jp[0][q] + wJp[1][i] * Jp[1][q];
+          if (d3) h += wJp[2][i] * Jp[2][q];
+          acc[u6(i, q)] = h;
+        }
+        R bb = Jp[0][i] * om[0] + Jp[1][i] * om[1];
+        if (d3) bb += Jp[2][i] * om[2];
+        acc[21 + i] = bb;
+      }
+    }
+  }
+  if (ph >= 0) {
+    __shared__ R sh[kLinThreads / 32][32];
+    const R mine = warp_reduce_scatter32(acc);
+    sh[threadIdx.x >> 5][threadIdx.x & 31] = mine;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      R t = R(0);
+#pragma unroll
+      for (int w = 0; w < kLinThreads / 32; ++w) t += sh[w][threadIdx.x];
+      Ptrs<R>::p(B.partials)[(size_t)c * 32 + threadIdx.x] = t;
+    }
+  }
+}
+
+// Hpp / b_p: sum of the chunk partials of each free pose (warp per pose).
+template <typename R>
+__global__ void k_pose_reduce(Bufs B, int Kf) {
+  const int i = blockIdx.x;
+  const int lane = threadIdx.x;
+  if (i >= Kf) return;
+  const int c0 = B.pose_chunk_begin[i], c1 = B.pose_chunk_begin[i + 1];
+  R s = R(0);
+  for (int c = c0; c < c1; ++c) s += Ptrs<R>::p(B.partials)[(size_t)c * 32 + lane];
+  R* H = Ptrs<R>::p(B.Hpp) + (size_t)i * 36;
+  if (lane < 21) {
+    int a = 0, rem = lane;
+    while (rem >= 6 - a) {
+      rem -= 6 - a;
+      ++a;
+    }
+    const int bcol = a + rem;
+    H[a * 6 + bcol] = s;
+    H[bcol * 6 + a] = s;
+  } else if (lane < 27) {
+    Ptrs<R>::p(B.b)[6 * (size_t)i + (lane - 21)] = s;
+  }
+}
+
+// Hll / b_l: sum over the (<= a few) edges of each free point.
+template <typename R>
+__global__ void k_point_reduce(Bufs B, int Lf, int n) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= Lf) return;
+  const int e0 = B.pt_begin[l], e1 = B.pt_begin[l + 1];
+  R s[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) s[k] = R(0);
+  for (int e = e0; e < e1; ++e) {
+    const R* row = Ptrs<R>::p(B.rows) + (size_t)e * kRow + 18;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) s[k] += row[k];
+  }
+  R* H = Ptrs<R>::p(B.Hll) + (size_t)l * 6;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) H[k] = s[k];
+  R* b = Ptrs<R>::p(B.b) + n + 3 * (size_t)l;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) b[k] = s[6 + k];
+}
+
+// computeLambdaInit (optimization_algorithm_levenberg.cpp:145-157):
+// tau * max |H_jj| over every free vertex (poses and points).
+template <typename R>
+__global__ void k_lambda_init(Bufs B, int Kf, int Lf, double tau) {
+  __shared__ double sh[32];
+  double m = 0;
+  for (int i = threadIdx.x; i < 6 * Kf; i += blockDim.x)
+    m = fmax(m, fabs((double)Ptrs<R>::p(B.Hpp)[(size_t)(i / 6) * 36 + 7 * (i % 6)]));
+  for (int i = threadIdx.x; i < 3 * Lf; i += blockDim.x) {
+    const int d = i % 3;
+    m = fmax(m, fabs((double)Ptrs<R>::p(B.Hll)[(size_t)(i / 3) * 6 + (d == 0 ? 0 : d == 1 ? 3 : 5)]));
+  }
+  m = warp_max(m);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double r = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+    r = warp_max(r);
+    if (threadIdx.x == 0) {
+      B.lm->lambda = tau * r;
+      B.lm->ni = 2.0;
+    }
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ void damped_inverse(const R* Hu, R lam, R* Di) {
+  const R d00 = Hu[0] + lam, d01 = Hu[1], d02 = Hu[2], d11 = Hu[3] + lam, d12 = Hu[4], d22 = Hu[5] + lam;
+  const R c00 = d11 * d22 - d12 * d12;
+  const R c01 = d12 * d02 - d01 * d22;
+  const R c02 = d01 * d12 - d11 * d02;
+  const R det = d00 * c00 + d01 * c01 + d02 * c02;
+  const R id = R(1) / det;
+  Di[0] = c00 * id;
+  Di[1] = c01 * id;
+  Di[2] = c02 * id;
+  Di[3] = c01 * id;
+  Di[4] = (d00 * d22 - d02 * d02) * id;
+  Di[5] = (d02 * d01 - d00 * d12) * id;
+  Di[6] = c02 * id;
+  Di[7] = Di[5];
+  Di[8] = (d00 * d11 - d01 * d01) * id;
+}
+
+// Y_e = Hpl_e Dinv, q_e = Hpl_e Dinv b_l for every canonical edge with a free pose.
+template <typename R>
+__global__ void k_schur_edge(Bufs B, int Ec, int n) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= Ec) return;
+  if (B.canon_pose_h[e] < 0) return;
+  const int l = B.canon_point_h[e];
+  const R lam = (R)B.lm->lambda;
+  R Di[9];
+  damped_inverse<R>(Ptrs<R>::p(B.Hll) + (size_t)l * 6, lam, Di);
+  const R* bl = Ptrs<R>::p(B.b) + n + 3 * (size_t)l;
+  R db[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) db[i] = Di[3 * i] * bl[0] + Di[3 * i + 1] * bl[1] + Di[3 * i + 2] * bl[2];
+  const R* H = Ptrs<R>::p(B.rows) + (size_t)e * kRow;
+  R h[18];
+#pragma unroll
+  for (int k = 0; k < 18; ++k) h[k] = H[k];
+  R* o = Ptrs<R>::p(B.yq) + (size_t)e * kYQ;
+#pragma unroll
+  for (int r = 0; r < 6; ++r) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) o[r * 3 + c] = h[r * 3] * Di[c] + h[r * 3 + 1] * Di[3 + c] + h[r * 3 + 2] * Di[6 + c];
+    o[18 + r] = h[r * 3] * db[0] + h[r * 3 + 1] * db[1] + h[r * 3 + 2] * db[2];
+  }
+}
+
+// Reduced-camera block products over the pair list: one warp per chunk of
+// <= 256 pairs that all belong to one block; lanes accumulate whole 6x6
+// products in registers, then a reduce-scatter gives one partial per chunk.
+template <typename R>
+__global__ void __launch_bounds__(256) k_schur_pairs(Bufs B, int npc) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= npc) return;
+  const int p0 = B.pchunk_begin[warp], p1 = B.pchunk_begin[warp + 1];
+  R acc[32], acc2[4];
+#pragma unroll
+  for (int k = 0; k < 32; ++k) acc[k] = R(0);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) acc2[k] = R(0);
+  const R* yq = Ptrs<R>::p(B.yq);
+  const R* rows = Ptrs<R>::p(B.rows);
+  for (int p = p0 + lane; p < p1; p += 32) {
+    const int2 ij = B.pairs[p];
+    const R* Y = yq + (size_t)ij.x * kYQ;
+    const R* H = rows + (size_t)ij.y * kRow;
+    R y[18], h[18];
+#pragma unroll
+    for (int k = 0; k < 18; ++k) {
+      y[k] = Y[k];
+      h[k] = H[k];
+    }
+#pragma unroll
+    for (int r = 0; r < 6; ++r)
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        const R v = y[r * 3] * h[c * 3] + y[r * 3 + 1] * h[c * 3 + 1] + y[r * 3 + 2] * h[c * 3 + 2];
+        const int t = r * 6 + c;
+        if (t < 32)
+          acc[t] += v;
+        else
+          acc2[t - 32] += v;
+      }
+  }
+  const R mine = warp_reduce_scatter32(acc);
+  R* out = Ptrs<R>::p(B.ppart) + (size_t)warp * 36;
+  out[lane] = mine;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const R s = warp_sum(acc2[k]);
+    if (lane == 0) out[32 + k] = s;
+  }
+}
+
+// S_ab = [a == b](Hpp_a + lambda I) - sum of the block's chunk partials, into
+// the dense FP64 reduced camera matrix (lower triangle is what the
+// factorisation reads).
+template <typename R>
+__global__ void k_schur_assemble(Bufs B, int ld) {
+  const int blk = blockIdx.x;
+  const int t = threadIdx.x;
+  if (t >= 36) return;
+  const int a = B.block_ab[2 * blk], bb = B.block_ab[2 * blk + 1];
+  const int c0 = B.block_chunk_begin[blk], c1 = B.block_chunk_begin[blk + 1];
+  R v = R(0);
+  for (int c = c0; c < c1; ++c) v += Ptrs<R>::p(B.ppart)[(size_t)c * 36 + t];
+  const int r = t / 6, q = t % 6;
+  if (a == bb) {
+    const R h = Ptrs<R>::p(B.Hpp)[(size_t)a * 36 + t];
+    double d = (double)(h - v);
+    if (r == q) d += B.lm->lambda;
+    B.S[(size_t)(6 * a + r) * ld + 6 * a + q] = d;
+  } else {
+    const double d = (double)(-v);
+    B.S[(size_t)(6 * a + r) * ld + 6 * bb + q] = d;
+    B.S[(size_t)(6 * bb + q) * ld + 6 * a + r] = d;
+  }
+}
+
+// b_schur = b_p - sum_e q_e over the pose's canonical edges, written as the
+// extra row of the factorised matrix.
+template <typename R>
+__global__ void k_bschur(Bufs B, int ld) {
+  const int a = blockIdx.x;
+  __shared__ R sh[32];
+  const int e0 = B.pose_canon_begin[a], e1 = B.pose_canon_begin[a + 1];
+  R s[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) s[k] = R(0);
+  for (int i = e0 + threadIdx.x; i < e1; i += blockDim.x) {
+    const R* q = Ptrs<R>::p(B.yq) + (size_t)B.pose_canon_list[i] * kYQ + 18;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) s[k] += q[k];
+  }
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const R tot = block_sum(s[k], sh);
+    if (threadIdx.x == 0) {
+      const R bp = Ptrs<R>::p(B.b)[6 * (size_t)a + k];
+      B.S[(size_t)ld * ld + 6 * a + k] = (double)(bp - tot);
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------ blocked Cholesky --
+// Diagonal tile k: LL^T in shared memory; a pivot <= 0 marks the solve as
+// failed (SimplicialLLT's info() != Success, linear_solver_eigen.h:118-126).
+__global__ void __launch_bounds__(256) k_chol_potrf(double* S, int ld, int k, LMState* lm) {
+  __shared__ double T[kNB][kNB + 1];
+  const int o = k * kNB;
+  for (int idx = threadIdx.x; idx < kNB * kNB; idx += blockDim.x) {
+    const int i = idx / kNB, j = idx % kNB;
+    T[i][j] = (j <= i) ? S[(size_t)(o + i) * ld + o + j] : 0.0;
+  }
+  __syncthreads();
+  for (int kk = 0; kk < kNB; ++kk) {
+    if (threadIdx.x == 0) {
+      const double d = T[kk][kk];
+      if (d <= 0.0) lm->solve_ok = 0;
+      T[kk][kk] = sqrt(d);
+    }
+    __syncthreads();
+    if (threadIdx.x > kk && threadIdx.x < kNB) T[threadIdx.x][kk] /= T[kk][kk];
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < kNB * kNB; idx += blockDim.x) {
+      const int i = idx / kNB, j = idx % kNB;
+      if (j > kk && i >= j) T[i][j] -= T[i][kk] * T[j][kk];
+    }
+    __syncthreads();
+  }
+  for (int idx = threadIdx.x; idx < kNB * kNB; idx += blockDim.x) {
+    const int i = idx / kNB, j = idx % kNB;
+    if (j <= i) S[(size_t)(o + i) * ld + o + j] = T[i][j];
+  }
+}
+
+// Rows below the diagonal tile (8 rows per CTA, the extra b row included):
+// L_ik = A_ik L_kk^-T.
+__global__ void __launch_bounds__(256) k_chol_trsm(double* S, int ld, int k, int nrows) {
+  __shared__ double L[kNB][kNB + 1];
+  __shared__ double X[8][kNB + 1];
+  const int o = k * kNB;
+  const int row0 = o + kNB + blockIdx.x * 8;
+  for (int idx = threadIdx.x; idx < kNB * kNB; idx += blockDim.x) {
+    const int i = idx / kNB, j = idx % kNB;
+    L[i][j] = (j <= i) ? S[(size_t)(o + i) * ld + o + j] : 0.0;
+  }
+  const int r = threadIdx.x / kNB, c = threadIdx.x % kNB;
+  const int grow = row0 + r;
+  X[r][c] = (grow < nrows) ? S[(size_t)grow * ld + o + c] : 0.0;
+  __syncthreads();
+  for (int kk = 0; kk < kNB; ++kk) {
+    if (c == kk) X[r][kk] /= L[kk][kk];
+    __syncthreads();
+    if (c > kk) X[r][c] -= X[r][kk] * L[c][kk];
+    __syncthreads();
+  }
+  if (grow < nrows) S[(size_t)grow * ld + o + c] = X[r][c];
+}
+
+// Trailing update A_ij -= L_ik L_jk^T on 8x8 sub-tiles of the lower part.
+__global__ void __launch_bounds__(64) k_chol_syrk(double* S, int ld, int k, int nrows) {
+  const int o = k * kNB;
+  const int base = o + kNB;
+  const int sc = blockIdx.x, sr = blockIdx.y;  // sub-tile column / row (8-wide) from base
+  const int col0 = base + sc * 8, row0 = base + sr * 8;
+  if (col0 > row0 + 7 || col0 >= ld) return;
+  __shared__ double Li[8][kNB + 1], Lj[8][kNB + 1];
+  for (int idx = threadIdx.x; idx < 8 * kNB; idx += blockDim.x) {
+    const int rr = idx / kNB, cc = idx % kNB;
+    Li[rr][cc] = (row0 + rr < nrows) ? S[(size_t)(row0 + rr) * ld + o + cc] : 0.0;
+    Lj[rr][cc] = S[(size_t)(col0 + rr) * ld + o + cc];
+  }
+  __syncthreads();
+  const int rr = threadIdx.x / 8, cc = threadIdx.x % 8;
+  const int grow = row0 + rr, gcol = col0 + cc;
+  if (grow >= nrows || gcol > grow) return;
+  double s = 0.0;
+#pragma unroll 8
+  for (int q = 0; q < kNB; ++q) s += Li[rr][q] * Lj[cc][q];
+  S[(size_t)grow * ld + gcol] -= s;
+}
+
+// L^T x = y with y in the extra row; writes x_p when the factorisation succeeded.
+__global__ void __launch_bounds__(256) k_chol_backsolve(const double* S, int ld, int n, double* x, LMState* lm) {
+  if (!lm->solve_ok) return;
+  __shared__ double xs[4096 + kNB];
+  __shared__ double part[8][kNB];
+  const double* y = S + (size_t)ld * ld;
+  const int nt = ld / kNB;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int I = nt - 1; I >= 0; --I) {
+    const int o = I * kNB;
+    double acc = 0.0;
+    for (int kr = o + kNB + wid; kr < ld; kr += 8) acc += S[(size_t)kr * ld + o + lane] * xs[kr];
+    part[wid][lane] = acc;
+    __syncthreads();
+    if (wid == 0) {
+      double rc = y[o + lane];
+#pragma unroll
+      for (int w = 0; w < 8; ++w) rc -= part[w][lane];
+      for (int c = kNB - 1; c >= 0; --c) {
+        const double xc = __shfl_sync(0xffffffffu, rc / S[(size_t)(o + c) * ld + o + c], c);
+        if (lane < c) rc -= S[(size_t)(o + c) * ld + o + lane] * xc;
+        if (lane == c) xs[o + c] = xc;
+      }
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = xs[i];
+}
+
+// Landmark back-substitution (block_solver.hpp:420-446) and point update,
+// plus the point part of computeScale (optimization_algorithm_levenberg.cpp:159-165).
+template <typename R>
+__global__ void k_backsub(Bufs B, int Lf, int n) {
+  __shared__ double sh[32];
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  const int cur = B.lm->cur, cand = cur ^ 1;
+  const double lam = B.lm->lambda;
+  double sc = 0.0;
+  if (l < Lf) {
+    double* xl = B.x + n + 3 * (size_t)l;
+    const R* bl = Ptrs<R>::p(B.b) + n + 3 * (size_t)l;
+    if (B.lm->solve_ok) {
+      R cl[3] = {bl[0], bl[1], bl[2]};
+      for (int e = B.pt_begin[l]; e < B.pt_begin[l + 1]; ++e) {
+        const int ph = B.canon_pose_h[e];
+        if (ph < 0) continue;
+        const R* H = Ptrs<R>::p(B.rows) + (size_t)e * kRow;
+        const double* xp = B.x + 6 * (size_t)ph;
+        R xr[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) xr[k] = (R)xp[k];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          R t = R(0);
+#pragma unroll
+          for (int k = 0; k < 6; ++k) t += H[k * 3 + q] * xr[k];
+          cl[q] -= t;
+        }
+      }
+      R Di[9];
+      damped_inverse<R>(Ptrs<R>::p(B.Hll) + (size_t)l * 6, (R)lam, Di);
+#pragma unroll
+      for (int q = 0; q < 3; ++q) xl[q] = (double)(Di[3 * q] * cl[0] + Di[3 * q + 1] * cl[1] + Di[3 * q + 2] * cl[2]);
+    }
+    const int id = B.free_point_ids[l];
+    const double* X0 = B.Xd[cur] + 3 * (size_t)id;
+    double* X1 = B.Xd[cand] + 3 * (size_t)id;
+    double nx[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const double d = xl[q];
+      nx[q] = X0[q] + d;
+      X1[q] = nx[q];
+      sc += d * (lam * d + (double)bl[q]);
+    }
+    B.Xf[cand][id] = make_float4((float)nx[0], (float)nx[1], (float)nx[2], 0.f);
+  }
+  const double tot = block_sum(sc, sh);
+  if (threadIdx.x == 0) B.scale_part[blockIdx.x] = tot;
+}
+
+// VertexSE3Expmap::oplusImpl on every free pose into the candidate buffer,
+// plus the pose part of computeScale.  Written to scale_part[slot].
+template <typename R>
+__global__ void k_update_poses(Bufs B, int Kf, int slot0) {
+  __shared__ double sh[32];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int cur = B.lm->cur, cand = cur ^ 1;
+  const double lam = B.lm->lambda;
+  double sc = 0.0;
+  if (i < Kf) {
+    const int id = B.free_pose_ids[i];
+    const double* u = B.x + 6 * (size_t)i;
+    double out[7];
+    se3_exp_left(u, B.pose_qt[cur] + 8 * (size_t)id, out);
+    double* dst = B.pose_qt[cand] + 8 * (size_t)id;
+#pragma unroll
+    for (int k = 0; k < 7; ++k) dst[k] = out[k];
+    double Rm[9];
+    quat_to_R(out, Rm);
+    PoseLinD d;
+    PoseLinF f;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      d.R[k] = Rm[k];
+      f.R[k] = (float)Rm[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      d.t[k] = out[4 + k];
+      f.c[k] = (float)(-(Rm[k] * out[4] + Rm[3 + k] * out[5] + Rm[6 + k] * out[6]));
+    }
+    B.pd[cand][id] = d;
+    B.pf[cand][id] = f;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) sc += u[k] * (lam * u[k] + (double)Ptrs<R>::p(B.b)[6 * (size_t)i + k]);
+  }
+  const double tot = block_sum(sc, sh);
+  if (threadIdx.x == 0) B.scale_part[slot0 + blockIdx.x] = tot;
+}
+
+// activeRobustChi2 (sparse_optimizer.cpp:102-116) at the current (which = 0)
+// or candidate (which = 1) state: one partial per CTA.
+template <typename R>
+__global__ void __launch_bounds__(256) k_cost(Bufs B, int E, int which) {
+  __shared__ double sh[32];
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const StateView v = make_view(B, B.lm->cur ^ which);
+  double rho = 0.0;
+  if (j < E) {
+    const EdgeRec r = B.recs[j];
+    const float obs[3] = {B.obs[3 * (size_t)j], B.obs[3 * (size_t)j + 1], B.obs[3 * (size_t)j + 2]};
+    R Pb[3], Pc[3], e[3], chi2;
+    transform(r, v, Pb, Pc);
+    edge_error<R>(r, obs, v, Pc, e, chi2);
+    rho = r.robust ? (double)huber_rho<R>(chi2, (R)r.delta) : (double)chi2;
+  }
+  const double tot = block_sum(rho, sh);
+  if (threadIdx.x == 0) B.cost_part[blockIdx.x] = tot;
+}
+
+__device__ double sum_partials(const double* p, int n, double* sh) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += p[i];
+  return block_sum(s, sh);
+}
+
+__global__ void k_lm_begin(Bufs B, int ncost) {
+  __shared__ double sh[32];
+  const double c = sum_partials(B.cost_part, ncost, sh);
+  if (threadIdx.x == 0) {
+    B.lm->current_chi = c;
+    B.lm->initial_chi = c;
+  }
+}
+
+__global__ void k_trial_begin(LMState* lm) {
+  if (threadIdx.x == 0) lm->solve_ok = 1;
+}
+
+// One LM trial's decision (optimization_algorithm_levenberg.cpp:113-141).
+__global__ void k_lm_decide(Bufs B, int ncost, int nscale) {
+  __shared__ double sh[32];
+  const double tempChi0 = sum_partials(B.cost_part, ncost, sh);
+  __syncthreads();
+  const double scale0 = sum_partials(B.scale_part, nscale, sh);
+  if (threadIdx.x != 0) return;
+  LMState* lm = B.lm;
+  const double chi_before = lm->current_chi;
+  double tempChi = tempChi0;
+  if (!lm->solve_ok) tempChi = DBL_MAX;
+  double rho = lm->current_chi - tempChi;
+  double scale = scale0 + 1e-3;
+  rho /= scale;
+  const double lam_used = lm->lambda;
+  const bool accepted = (rho > 0) && isfinite(tempChi);
+  bool brk = false;
+  if (accepted) {
+    double alpha = 1. - pow((2 * rho - 1), 3);
+    alpha = fmin(alpha, 2. / 3.);
+    const double sf = fmax(1. / 3., alpha);
+    lm->lambda *= sf;
+    lm->ni = 2;
+    lm->current_chi = tempChi;
+    lm->cur ^= 1;
+  } else {
+    lm->lambda *= lm->ni;
+    lm->ni *= 2;
+    if (!isfinite(lm->lambda)) brk = true;
+  }
+  if (lm->n_log < lm->max_log) {
+    mcba_trial_log& L = B.log[lm->n_log];
+    L.iteration = lm->iteration;
+    L.trial = lm->trial;
+    L.chi_before = chi_before;
+    L.chi_after = tempChi;
+    L.lambda = lam_used;
+    L.scale = scale;
+    L.rho = rho;
+    L.accepted = accepted ? 1 : 0;
+    L.solve_ok = lm->solve_ok;
+  }
+  lm->n_log++;
+  lm->total_trials++;
+  lm->temp_chi = tempChi;
+  lm->rho = rho;
+  lm->scale = scale;
+  lm->last_accepted = accepted ? 1 : 0;
+  if (!brk) lm->trial++;
+  const bool more = !brk && rho < 0 && lm->trial < lm->max_trials;
+  lm->trial_continue = more ? 1 : 0;
+  if (!more) {
+    if (lm->trial == lm->max_trials || rho == 0 || !isfinite(lm->lambda)) lm->terminate = 1;
+    lm->iteration++;
+  }
+}
+
+__global__ void k_iter_begin(LMState* lm) {
+  if (threadIdx.x == 0) {
+    lm->trial = 0;
+    lm->trial_continue = 1;
+  }
+}
+
+// Zero the reduced camera matrix storage and put ones on the padding diagonal.
+__global__ void k_init_S(double* S, int ld, int n, size_t total) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = i / ld, c = i % ld;
+    S[i] = (r == c && (int)r >= n && (int)r < ld) ? 1.0 : 0.0;
+  }
+}
+
+__global__ void k_edge_chi2(const EdgeRec* recs, const float* obs, int E, StateView v, double* out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= E) return;
+  const EdgeRec r = recs[j];
+  const float o[3] = {obs[3 * (size_t)j], obs[3 * (size_t)j + 1], obs[3 * (size_t)j + 2]};
+  double Pb[3], Pc[3], e[3], chi2;
+  transform(r, v, Pb, Pc);
+  edge_error<double>(r, o, v, Pc, e, chi2);
+  out[j] = chi2;
+}
+
+}  // namespace
+
+// ----------------------------------------------------------- host side --
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t n) {
+    if (n <= cap && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    const size_t want = std::max<size_t>(n, 1);
+    cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+namespace {
+struct Launch {
+  int nchunk, Kf, Lf, Ec, E, n, npc, nblk, ld, nrows, ncost, nscale_pts, nscale_pose, tiles;
+  int K, P, NP;
+};
+}  // namespace
+
+class Solver {
+ public:
+  int device = 0;
+  int precision = MCBA_PREC_FP64;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  // state
+  DBuf<double> pose_qt[2], Xd[2], pose_qt0, Xd0;
+  DBuf<PoseLinD> pd[2];
+  DBuf<PoseLinF> pf[2];
+  DBuf<float4> Xf[2];
+  DBuf<CamD> cd;
+  DBuf<CamF> cf;
+  // structure
+  DBuf<EdgeRec> recs, recs_all;
+  DBuf<float> obs, obs_all;
+  DBuf<int> chunk_begin, chunk_pose, pose_chunk_begin, pt_begin, canon_pose_h, canon_point_h, pchunk_begin,
+      block_ab, block_chunk_begin, pose_canon_begin, pose_canon_list, free_pose_ids, free_point_ids;
+  DBuf<int2> pairs;
+  // numerics
+  DBuf<char> rows, partials, Hpp, Hll, b, yq, ppart;
+  DBuf<double> S, x, cost_part, scale_part, chi2_out;
+  DBuf<LMState> lm;
+  DBuf<mcba_trial_log> log;
+  LMState* lm_host = nullptr;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  std::vector<cudaEvent_t> evpool;
+  size_t evnext = 0;
+  Launch L{};
+  bool uploaded = false;
+  int64_t launches = 0;
+
+  cudaEvent_t next_event() {
+    if (evnext == evpool.size()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      evpool.push_back(e);
+    }
+    return evpool[evnext++];
+  }
+
+  ~Solver() {
+    cudaSetDevice(device);
+    if (stream) cudaStreamSynchronize(stream);
+    DBuf<double>* ds[] = {&pose_qt[0], &pose_qt[1], &Xd[0], &Xd[1], &pose_qt0, &Xd0,
+                          &S, &x, &cost_part, &scale_part, &chi2_out};
+    for (auto* d : ds) d->release();
+    pd[0].release();
+    pd[1].release();
+    pf[0].release();
+    pf[1].release();
+    Xf[0].release();
+    Xf[1].release();
+    cd.release();
+    cf.release();
+    recs.release();
+    recs_all.release();
+    obs.release();
+    obs_all.release();
+    DBuf<int>* is[] = {&chunk_begin, &chunk_pose, &pose_chunk_begin, &pt_begin, &canon_pose_h, &canon_point_h,
+                       &pchunk_begin, &block_ab, &block_chunk_begin, &pose_canon_begin, &pose_canon_list,
+                       &free_pose_ids, &free_point_ids};
+    for (auto* d : is) d->release();
+    pairs.release();
+    DBuf<char>* cs[] = {&rows, &partials, &Hpp, &Hll, &b, &yq, &ppart};
+    for (auto* d : cs) d->release();
+    lm.release();
+    log.release();
+    if (lm_host) cudaFreeHost(lm_host);
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+    for (auto& e : evpool) cudaEventDestroy(e);
+    if (own_stream && stream) cudaStreamDestroy(stream);
+  }
+};
+
+#define CK(call)                                                                   \
+  do {                                                                             \
+    cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess) {                                                       \
+      if (err) *err = std::string(#call) + ": " + cudaGetErrorString(e_);          \
+      return MCBA_ERR_CUDA;                                                        \
+    }                                                                              \
+  } while (0)
+
+Solver* solver_create(int device, int precision, void* stream, std::string* err) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    if (err) *err = "no CUDA device";
+    return nullptr;
+  }
+  if (device < 0 || device >= n) {
+    if (err) *err = "no CUDA device with that ordinal";
+    return nullptr;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) {
+    if (err) *err = "cudaSetDevice failed";
+    return nullptr;
+  }
+  Solver* s = new Solver();
+  s->device = device;
+  s->precision = precision;
+  if (stream) {
+    s->stream = (cudaStream_t)stream;
+  } else {
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete s;
+      if (err) *err = "cudaStreamCreate failed";
+      return nullptr;
+    }
+    s->own_stream = true;
+  }
+  if (cudaMallocHost(&s->lm_host, sizeof(LMState)) != cudaSuccess) {
+    delete s;
+    if (err) *err = "cudaMallocHost failed";
+    return nullptr;
+  }
+  for (auto& e : s->ev) cudaEventCreate(&e);
+  return s;
+}
+
+void solver_destroy(Solver* s) { delete s; }
+bool solver_has_upload(const Solver* s) { return s && s->uploaded; }
+
+namespace {
+
+template <typename T>
+cudaError_t up(DBuf<T>& d, const std::vector<T>& h, cudaStream_t st, int64_t& bytes) {
+  cudaError_t e = d.ensure(h.size());
+  if (e != cudaSuccess || h.empty()) return e;
+  bytes += (int64_t)(h.size() * sizeof(T));
+  return cudaMemcpyAsync(d.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, st);
+}
+
+void cam_to_dev(const HostCamera& c, CamD& d, CamF& f) {
+  const double* q = c.T_cb.q;
+  const double x = q[0], y = q[1], z = q[2], w = q[3];
+  const double tx = 2 * x, ty = 2 * y, tz = 2 * z;
+  const double Rm[9] = {1 - (ty * y + tz * z), ty * x - tz * w, tz * x + ty * w,
+                        ty * x + tz * w,       1 - (tx * x + tz * z), tz * y - tx * w,
+                        tz * x - ty * w,       tz * y + tx * w,       1 - (tx * x + ty * y)};
+  for (int k = 0; k < 4; ++k) {
+    d.K[k] = c.K[k];
+    f.K[k] = c.K[k];
+  }
+  d.bf = c.bf;
+  f.bf = c.bf;
+  for (int k = 0; k < 9; ++k) {
+    d.R[k] = Rm[k];
+    f.R[k] = (float)Rm[k];
+  }
+  for (int k = 0; k < 3; ++k) {
+    d.t[k] = c.T_cb.t[k];
+    f.t[k] = (float)c.T_cb.t[k];
+  }
+}
+
+// Both halves of the double-buffered state from the buffer-0 copy (or from
+// the saved initial state), with the derived rotation matrices / float copies.
+int spread_state(Solver* s, bool from_initial, std::string* err) {
+  const Launch& L = s->L;
+  cudaStream_t st = s->stream;
+  for (int b = 0; b < 2; ++b) {
+    const double* srcq = from_initial ? s->pose_qt0.p : s->pose_qt[0].p;
+    const double* srcx = from_initial ? s->Xd0.p : s->Xd[0].p;
+    if (from_initial || b == 1) {
+      if (L.K) CK(cudaMemcpyAsync(s->pose_qt[b].p, srcq, 8 * (size_t)L.K * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      if (L.NP) CK(cudaMemcpyAsync(s->Xd[b].p, srcx, 3 * (size_t)L.NP * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    }
+    if (L.K) {
+      k_pose_lin<<<(L.K + 127) / 128, 128, 0, st>>>(s->pose_qt[b].p, L.K, s->pd[b].p, s->pf[b].p);
+      s->launches++;
+    }
+    if (L.NP) {
+      k_points_f<<<(L.NP + 255) / 256, 256, 0, st>>>(s->Xd[b].p, L.NP, s->Xf[b].p);
+      s->launches++;
+    }
+  }
+  CK(cudaGetLastError());
+  return MCBA_OK;
+}
+
+int upload_state(Solver* s, const HostProblem& hp, int U, int64_t& bytes, std::string* err) {
+  const int K = (int)hp.poses.size();
+  const int P = (int)hp.point_fixed.size();
+  std::vector<double> q(8 * (size_t)std::max(K, 1), 0.0);
+  for (int k = 0; k < K; ++k) {
+    for (int i = 0; i < 4; ++i) q[8 * k + i] = hp.poses[k].q[i];
+    for (int i = 0; i < 3; ++i) q[8 * k + 4 + i] = hp.poses[k].t[i];
+  }
+  std::vector<double> X(3 * (size_t)(P + U) + 3, 0.0);
+  std::copy(hp.points.begin(), hp.points.end(), X.begin());
+  {
+    int u = 0;
+    for (size_t i = 0; i < hp.n_edges(); ++i)
+      if (hp.e_type[i] == MCBA_EDGE_UNARY) {
+        for (int d = 0; d < 3; ++d) X[3 * (size_t)(P + u) + d] = hp.e_Xw[3 * i + d];
+        ++u;
+      }
+  }
+  std::vector<CamD> cd(hp.cams.size());
+  std::vector<CamF> cf(hp.cams.size());
+  for (size_t c = 0; c < hp.cams.size(); ++c) cam_to_dev(hp.cams[c], cd[c], cf[c]);
+  CK(up(s->cd, cd, s->stream, bytes));
+  CK(up(s->cf, cf, s->stream, bytes));
+  const int NP = P + U;
+  CK(up(s->pose_qt[0], q, s->stream, bytes));
+  CK(up(s->Xd[0], X, s->stream, bytes));
+  CK(s->pose_qt[1].ensure(q.size()));
+  CK(s->Xd[1].ensure(X.size()));
+  CK(s->pose_qt0.ensure(q.size()));
+  CK(s->Xd0.ensure(X.size()));
+  for (int b = 0; b < 2; ++b) {
+    CK(s->pd[b].ensure(std::max(K, 1)));
+    CK(s->pf[b].ensure(std::max(K, 1)));
+    CK(s->Xf[b].ensure(std::max(NP, 1)));
+  }
+  s->L.K = K;
+  s->L.P = P;
+  s->L.NP = NP;
+  if (K) CK(cudaMemcpyAsync(s->pose_qt0.p, s->pose_qt[0].p, 8 * (size_t)K * sizeof(double), cudaMemcpyDeviceToDevice, s->stream));
+  if (NP) CK(cudaMemcpyAsync(s->Xd0.p, s->Xd[0].p, 3 * (size_t)NP * sizeof(double), cudaMemcpyDeviceToDevice, s->stream));
+  return spread_state(s, false, err);
+}
+
+Bufs make_bufs(Solver* s) {
+  Bufs B;
+  for (int i = 0; i < 2; ++i) {
+    B.pose_qt[i] = s->pose_qt[i].p;
+    B.pd[i] = s->pd[i].p;
+    B.pf[i] = s->pf[i].p;
+    B.Xd[i] = s->Xd[i].p;
+    B.Xf[i] = s->Xf[i].p;
+  }
+  B.cd = s->cd.p;
+  B.cf = s->cf.p;
+  B.recs = s->recs.p;
+  B.obs = s->obs.p;
+  B.chunk_begin = s->chunk_begin.p;
+  B.chunk_pose = s->chunk_pose.p;
+  B.pose_chunk_begin = s->pose_chunk_begin.p;
+  B.pt_begin = s->pt_begin.p;
+  B.canon_pose_h = s->canon_pose_h.p;
+  B.canon_point_h = s->canon_point_h.p;
+  B.pairs = s->pairs.p;
+  B.pchunk_begin = s->pchunk_begin.p;
+  B.block_ab = s->block_ab.p;
+  B.block_chunk_begin = s->block_chunk_begin.p;
+  B.pose_canon_begin = s->pose_canon_begin.p;
+  B.pose_canon_list = s->pose_canon_list.p;
+  B.free_pose_ids = s->free_pose_ids.p;
+  B.free_point_ids = s->free_point_ids.p;
+  B.rows = s->rows.p;
+  B.partials = s->partials.p;
+  B.Hpp = s->Hpp.p;
+  B.Hll = s->Hll.p;
+  B.b = s->b.p;
+  B.yq = s->yq.p;
+  B.ppart = s->ppart.p;
+  B.S = s->S.p;
+  B.x = s->x.p;
+  B.cost_part = s->cost_part.p;
+  B.scale_part = s->scale_part.p;
+  B.lm = s->lm.p;
+  B.log = s->log.p;
+  return B;
+}
+
+// Per-phase CUDA-event timing (profile option).
+struct PhaseClock {
+  Solver* s;
+  bool on;
+  struct Rec {
+    int phase;
+    cudaEvent_t a, b;
+  };
+  std::vector<Rec> pending;
+  template <typename F>
+  void run(int phase, F&& fn) {
+    if (!on) {
+      fn();
+      return;
+    }
+    Rec r{phase, s->next_event(), s->next_event()};
+    cudaEventRecord(r.a, s->stream);
+    fn();
+    cudaEventRecord(r.b, s->stream);
+    pending.push_back(r);
+  }
+  // after a stream synchronisation
+  void collect(SolveResult& out) {
+    for (auto& r : pending) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+        out.ms_phase[r.phase] += ms;
+        out.n_phase[r.phase]++;
+      }
+    }
+    pending.clear();
+    s->evnext = 0;
+  }
+};
+
+template <typename R>
+void launch_linearize(Solver* s, const Bufs& B, const Launch& L, bool first, double tau, PhaseClock& pc) {
+  cudaStream_t st = s->stream;
+  pc.run(MCBA_PHASE_LINEARIZE, [&] {
+    k_linearize<R><<<L.nchunk, kLinThreads, 0, st>>>(B);
+    s->launches++;
+  });
+  pc.run(MCBA_PHASE_REDUCE, [&] {
+    if (L.Kf) {
+      k_pose_reduce<R><<<L.Kf, 32, 0, st>>>(B, L.Kf);
+      s->launches++;
+    }
+    if (L.Lf) {
+      k_point_reduce<R><<<(L.Lf + 127) / 128, 128, 0, st>>>(B, L.Lf, L.n);
+      s->launches++;
+    }
+    if (first) {
+      k_lambda_init<R><<<1, 256, 0, st>>>(B, L.Kf, L.Lf, tau);
+      s->launches++;
+    }
+  });
+}
+
+template <typename R>
+void launch_trial(Solver* s, const Bufs& B, const Launch& L, PhaseClock& pc) {
+  cudaStream_t st = s->stream;
+  k_trial_begin<<<1, 32, 0, st>>>(B.lm);
+  s->launches++;
+  if (L.Kf) {
+    pc.run(MCBA_PHASE_SCHUR_EDGE, [&] {
+      if (L.Ec) {
+        k_schur_edge<R><<<(L.Ec + 127) / 128, 128, 0, st>>>(B, L.Ec, L.n);
+        s->launches++;
+      }
+    });
+    pc.run(MCBA_PHASE_SCHUR_PAIRS, [&] {
+      if (L.npc) {
+        k_schur_pairs<R><<<(L.npc + 7) / 8, 256, 0, st>>>(B, L.npc);
+        s->launches++;
+      }
+    });
+    pc.run(MCBA_PHASE_SCHUR_ASSEMBLE, [&] {
+      k_schur_assemble<R><<<L.nblk, 64, 0, st>>>(B, L.ld);
+      k_bschur<R><<<L.Kf, 256, 0, st>>>(B, L.ld);
+      s->launches += 2;
+    });
+    pc.run(MCBA_PHASE_CHOLESKY, [&] {
+      for (int k = 0; k < L.tiles; ++k) {
+        k_chol_potrf<<<1, 256, 0, st>>>(B.S, L.ld, k, B.lm);
+        s->launches++;
+        const int below = L.nrows - (k + 1) * kNB;
+        if (below > 0) {
+          k_chol_trsm<<<(below + 7) / 8, 256, 0, st>>>(B.S, L.ld, k, L.nrows);
+          s->launches++;
+          const int rem_cols = L.ld - (k + 1) * kNB;
+          if (rem_cols > 0) {
+            dim3 g(rem_cols / 8, (below + 7) / 8);
+            k_chol_syrk<<<g, 64, 0, st>>>(B.S, L.ld, k, L.nrows);
+            s->launches++;
+          }
+        }
+      }
+      k_chol_backsolve<<<1, 256, 0, st>>>(B.S, L.ld, L.n, B.x, B.lm);
+      s->launches++;
+    });
+  }
+  pc.run(MCBA_PHASE_UPDATE, [&] {
+    k_backsub<R><<<L.nscale_pts, 128, 0, st>>>(B, L.Lf, L.n);
+    k_update_poses<R><<<L.nscale_pose, 128, 0, st>>>(B, L.Kf, L.nscale_pts);
+    s->launches += 2;
+  });
+  pc.run(MCBA_PHASE_COST, [&] {
+    k_cost<R><<<L.ncost, 256, 0, st>>>(B, L.E, 1);
+    k_lm_decide<<<1, 256, 0, st>>>(B, L.ncost, L.nscale_pts + L.nscale_pose);
+    s->launches += 2;
+  });
+}
+
+template <typename R>
+int alloc_numerics(Solver* s, const Structure& st, std::string* err) {
+  const Launch& L = s->L;
+  const size_t rb = sizeof(R);
+  const int nx = L.n + 3 * L.Lf;
+  CK(s->rows.ensure(std::max<size_t>(1, (size_t)st.Ec * kRow * rb)));
+  CK(s->partials.ensure(std::max<size_t>(1, (size_t)L.nchunk * 32 * rb)));
+  CK(s->Hpp.ensure(std::max<size_t>(1, (size_t)L.Kf * 36 * rb)));
+  CK(s->Hll.ensure(std::max<size_t>(1, (size_t)L.Lf * 6 * rb)));
+  CK(s->b.ensure(std::max<size_t>(1, (size_t)nx * rb)));
+  CK(s->yq.ensure(std::max<size_t>(1, (size_t)st.Ec * kYQ * rb)));
+  CK(s->ppart.ensure(std::max<size_t>(1, (size_t)L.npc * 36 * rb)));
+  CK(s->S.ensure((size_t)(L.ld + kNB) * L.ld));
+  CK(s->x.ensure(std::max(nx, 1)));
+  CK(s->cost_part.ensure(L.ncost));
+  CK(s->scale_part.ensure(L.nscale_pts + L.nscale_pose));
+  CK(s->lm.ensure(1));
+  return MCBA_OK;
+}
+
+template <typename R>
+int run_lm(Solver* s, const RunOptions& o, SolveResult& out, std::string* err) {
+  const Launch& L = s->L;
+  cudaStream_t stm = s->stream;
+  const int nx = L.n + 3 * L.Lf;
+  const int iterations = o.iterations, max_trials = o.max_trials;
+  const int max_log = std::max(1, iterations * max_trials);
+  CK(s->log.ensure(max_log));
+  // S: identity padding, zero b row
+  {
+    const size_t total = (size_t)(L.ld + kNB) * L.ld;
+    k_init_S<<<(int)std::min<size_t>((total + 255) / 256, 4096), 256, 0, stm>>>(s->S.p, L.ld, L.n, total);
+    s->launches++;
+  }
+  CK(cudaMemsetAsync(s->x.p, 0, std::max(nx, 1) * sizeof(double), stm));
+  LMState init{};
+  init.cur = 0;
+  init.solve_ok = 1;
+  init.max_trials = max_trials;
+  init.max_log = max_log;
+  init.lambda = -1;
+  init.ni = 2;
+  *s->lm_host = init;
+  CK(cudaMemcpyAsync(s->lm.p, s->lm_host, sizeof(LMState), cudaMemcpyHostToDevice, stm));
+  out.h2d += sizeof(LMState);
+  Bufs B = make_bufs(s);
+  PhaseClock pc{s, o.profile, {}};
+
+  float ms_lin = 0.f;
+  CK(cudaEventRecord(s->ev[0], stm));
+  pc.run(MCBA_PHASE_COST, [&] {
+    k_cost<R><<<L.ncost, 256, 0, stm>>>(B, L.E, 0);
+    k_lm_begin<<<1, 256, 0, stm>>>(B, L.ncost);
+    s->launches += 2;
+  });
+  int it = 0;
+  bool stop = false;
+  for (it = 0; it < iterations && !stop; ++it) {
+    k_iter_begin<<<1, 32, 0, stm>>>(B.lm);
+    s->launches++;
+    CK(cudaEventRecord(s->ev[2], stm));
+    launch_linearize<R>(s, B, L, it == 0, o.tau, pc);
+    CK(cudaEventRecord(s->ev[3], stm));
+    for (int t = 0; t < max_trials; ++t) {
+      launch_trial<R>(s, B, L, pc);
+      CK(cudaGetLastError());
+      CK(cudaMemcpyAsync(s->lm_host, s->lm.p, sizeof(LMState), cudaMemcpyDeviceToHost, stm));
+      out.d2h += sizeof(LMState);
+      CK(cudaStreamSynchronize(stm));
+      pc.collect(out);
+      if (t == 0) {
+        float m = 0.f;
+        cudaEventElapsedTime(&m, s->ev[2], s->ev[3]);
+        ms_lin += m;
+      }
+      if (!s->lm_host->trial_continue) break;
+    }
+    if (s->lm_host->terminate) stop = true;
+  }
+  CK(cudaEventRecord(s->ev[1], stm));
+  CK(cudaMemcpyAsync(s->lm_host, s->lm.p, sizeof(LMState), cudaMemcpyDeviceToHost, stm));
+  out.d2h += sizeof(LMState);
+  CK(cudaStreamSynchronize(stm));
+  pc.collect(out);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, s->ev[0], s->ev[1]);
+  out.ms_total = ms;
+  out.ms_linearize = ms_lin;
+  out.iterations = it;
+  out.trials = s->lm_host->total_trials;
+  out.initial_chi2 = s->lm_host->initial_chi;
+  out.final_chi2 = s->lm_host->current_chi;
+  out.lambda = s->lm_host->lambda;
+  const int nl = std::min(s->lm_host->n_log, max_log);
+  out.log.resize(nl);
+  if (nl) {
+    CK(cudaMemcpy(out.log.data(), s->log.p, nl * sizeof(mcba_trial_log), cudaMemcpyDeviceToHost));
+    out.d2h += nl * sizeof(mcba_trial_log);
+  }
+  // Hpp of the last linearisation, FP64 on the host (DumpCalculationGraph)
+  if (L.Kf && iterations > 0) {
+    std::vector<R> h((size_t)L.Kf * 36);
+    CK(cudaMemcpy(h.data(), s->Hpp.p, h.size() * sizeof(R), cudaMemcpyDeviceToHost));
+    out.d2h += h.size() * sizeof(R);
+    out.hpp.assign(h.begin(), h.end());
+  }
+  return MCBA_OK;
+}
+
+}  // namespace
+
+int solver_upload(Solver* s, const HostProblem& hp, const Structure& st, SolveResult& out, std::string* err) {
+  CK(cudaSetDevice(s->device));
+  s->uploaded = false;
+  int64_t bytes = 0;
+  int r = upload_state(s, hp, st.U, bytes, err);
+  if (r) return r;
+  cudaStream_t stm = s->stream;
+  CK(up(s->recs, st.recs, stm, bytes));
+  CK(up(s->obs, st.obs, stm, bytes));
+  CK(up(s->chunk_begin, st.chunk_begin, stm, bytes));
+  CK(up(s->chunk_pose, st.chunk_pose, stm, bytes));
+  CK(up(s->pose_chunk_begin, st.pose_chunk_begin, stm, bytes));
+  CK(up(s->pt_begin, st.pt_begin, stm, bytes));
+  CK(up(s->canon_pose_h, st.canon_pose_h, stm, bytes));
+  CK(up(s->canon_point_h, st.canon_point_h, stm, bytes));
+  CK(s->pairs.ensure(std::max<size_t>(1, st.pair_ij.size() / 2)));
+  if (!st.pair_ij.empty()) {
+    CK(cudaMemcpyAsync(s->pairs.p, st.pair_ij.data(), st.pair_ij.size() * sizeof(int32_t), cudaMemcpyHostToDevice, stm));
+    bytes += st.pair_ij.size() * sizeof(int32_t);
+  }
+  CK(up(s->pchunk_begin, st.pchunk_begin, stm, bytes));
+  CK(up(s->block_ab, st.block_ab, stm, bytes));
+  CK(up(s->block_chunk_begin, st.block_chunk_begin, stm, bytes));
+  CK(up(s->pose_canon_begin, st.pose_canon_begin, stm, bytes));
+  CK(up(s->pose_canon_list, st.pose_canon_list, stm, bytes));
+  CK(up(s->free_pose_ids, st.free_pose_ids, stm, bytes));
+  CK(up(s->free_point_ids, st.free_point_ids, stm, bytes));
+  Launch& L = s->L;
+  const int Kf = st.Kf, Lf = st.Lf, n = 6 * Kf;
+  L.nchunk = (int)st.chunk_pose.size();
+  L.Kf = Kf;
+  L.Lf = Lf;
+  L.Ec = st.Ec;
+  L.E = st.E;
+  L.n = n;
+  L.npc = (int)st.pchunk_block.size();
+  L.nblk = (int)st.block_ab.size() / 2;
+  L.ld = std::max(kNB, ((n + kNB - 1) / kNB) * kNB);
+  L.tiles = L.ld / kNB;
+  L.nrows = L.ld + 1;  // the b_schur row
+  L.ncost = (st.E + 255) / 256;
+  L.nscale_pts = std::max(1, (Lf + 127) / 128);
+  L.nscale_pose = std::max(1, (Kf + 127) / 128);
+  if (L.ld > 4096) {
+    if (err) *err = "reduced camera system above 4096 (682 free keyframes)";
+    return MCBA_ERR_TOO_LARGE;
+  }
+  r = (s->precision == MCBA_PREC_MIXED) ? alloc_numerics<float>(s, st, err) : alloc_numerics<double>(s, st, err);
+  if (r) return r;
+  out.h2d += bytes;
+  s->uploaded = true;
+  return MCBA_OK;
+}
+
+int solver_run(Solver* s, const RunOptions& o, bool restore, SolveResult& out, std::string* err) {
+  if (!s->uploaded) {
+    if (err) *err = "no problem uploaded";
+    return MCBA_ERR_INVALID;
+  }
+  CK(cudaSetDevice(s->device));
+  if (restore) {
+    const int r = spread_state(s, true, err);
+    if (r) return r;
+  }
+  const int64_t l0 = s->launches;
+  const int r = (s->precision == MCBA_PREC_MIXED) ? run_lm<float>(s, o, out, err) : run_lm<double>(s, o, out, err);
+  out.launches += s->launches - l0;
+  return r;
+}
+
+int solver_download(Solver* s, HostProblem& hp, SolveResult& out, std::string* err) {
+  CK(cudaSetDevice(s->device));
+  const int K = (int)hp.poses.size(), P = (int)hp.point_fixed.size();
+  const int cur = s->lm_host->cur;
+  std::vector<double> q(8 * (size_t)std::max(K, 1));
+  if (K) {
+    CK(cudaMemcpy(q.data(), s->pose_qt[cur].p, 8 * (size_t)K * sizeof(double), cudaMemcpyDeviceToHost));
+    out.d2h += 8 * (int64_t)K * sizeof(double);
+  }
+  if (P) {
+    CK(cudaMemcpy(hp.points.data(), s->Xd[cur].p, 3 * (size_t)P * sizeof(double), cudaMemcpyDeviceToHost));
+    out.d2h += 3 * (int64_t)P * sizeof(double);
+  }
+  for (int k = 0; k < K; ++k) {
+    for (int i = 0; i < 4; ++i) hp.poses[k].q[i] = q[8 * k + i];
+    for (int i = 0; i < 3; ++i) hp.poses[k].t[i] = q[8 * k + 4 + i];
+  }
+  return MCBA_OK;
+}
+
+int solver_edge_chi2(Solver* s, const HostProblem& hp, std::vector<double>& chi2, std::string* err) {
+  CK(cudaSetDevice(s->device));
+  int U = 0;
+  for (size_t i = 0; i < hp.n_edges(); ++i)
+    if (hp.e_type[i] == MCBA_EDGE_UNARY) ++U;
+  int64_t bytes = 0;
+  s->uploaded = false;  // the state buffers are reused below
+  int r = upload_state(s, hp, U, bytes, err);
+  if (r) return r;
+  const int E = (int)hp.n_edges();
+  const int P = (int)hp.point_fixed.size();
+  std::vector<EdgeRec> recs(E);
+  std::vector<float> obs(3 * (size_t)E);
+  int u = 0;
+  for (int i = 0; i < E; ++i) {
+    EdgeRec& e = recs[i];
+    e.pose = hp.e_pose[i];
+    e.point = hp.e_type[i] == MCBA_EDGE_UNARY ? P + u++ : hp.e_point[i];
+    e.pose_h = -1;
+    e.point_h = -1;
+    e.canon = -1;
+    e.type = hp.e_type[i];
+    e.cam = (uint8_t)hp.e_cam[i];
+    e.robust = 0;
+    e.dim = e.type == MCBA_EDGE_STEREO ? 3 : 2;
+    e.info = hp.e_info[i];
+    e.delta = hp.e_delta[i];
+    for (int d = 0; d < 3; ++d) obs[3 * (size_t)i + d] = hp.e_obs[3 * (size_t)i + d];
+  }
+  cudaStream_t stm = s->stream;
+  CK(up(s->recs_all, recs, stm, bytes));
+  CK(up(s->obs_all, obs, stm, bytes));
+  CK(s->chi2_out.ensure(std::max(E, 1)));
+  StateView v;
+  v.pd = s->pd[0].p;
+  v.pf = s->pf[0].p;
+  v.Xd = s->Xd[0].p;
+  v.Xf = s->Xf[0].p;
+  v.cd = s->cd.p;
+  v.cf = s->cf.p;
+  if (E) k_edge_chi2<<<(E + 255) / 256, 256, 0, stm>>>(s->recs_all.p, s->obs_all.p, E, v, s->chi2_out.p);
+  CK(cudaGetLastError());
+  chi2.resize(E);
+  if (E) CK(cudaMemcpyAsync(chi2.data(), s->chi2_out.p, E * sizeof(double), cudaMemcpyDeviceToHost, stm));
+  CK(cudaStreamSynchronize(stm));
+  return MCBA_OK;
+}
+
+}  // namespace mcba
+
+extern "C" int mcba_device_count(int* count) {
+  if (!count) return MCBA_ERR_INVALID;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) n = 0;
+  *count = n;
+  return MCBA_OK;
+}

@@ -1,0 +1,449 @@
+"""Seeded synthetic bundle-adjustment problems for the multi-camera rig.
+
+The reference measures its local BA on an OpenSceneGraph-rendered drone
+sequence that is not available; these generators stand in for it with the
+shapes, sizes and noise model of the benchmark configurations:
+
+* rig: left/right 640x480 cameras yawed 30 deg outward at x = 0 and x = 1.0 m,
+  a 1280x720 wide camera (110 deg HFOV) at x = 0.5 m, all on one body;
+* a smooth random drone trajectory (0.3 m steps, at most 5 deg per step);
+* map points uniform in a 20 x 20 x 10 m box;
+* every in-image projection with depth > 0.5 m kept, 2..8 per point;
+* pixel noise N(0, 1 px^2), a fraction replaced by uniform outliers;
+* initial poses perturbed N(0, 0.05 m / 1 deg), points N(0, 0.1 m);
+* the first two keyframes fixed (and left unperturbed).
+
+Everything crosses the boundary the way the reference hands it to
+``BAoptimizer``: poses as float 4x4 T_body_world (``Frame::GetPose``), points
+as float[3], observations as float pixels, information as float invSigma2,
+Huber thresholds as float (include/BAoptimizer.hpp:62-63).
+
+Body/camera frames follow the camera convention (x right, y down, z forward).
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+from typing import Optional
+
+import numpy as np
+
+EDGE_MONO = 0
+EDGE_STEREO = 1
+EDGE_UNARY = 2
+
+HUBER_BENCH = np.float32(math.sqrt(5.991))   # delta used by the benchmark configs
+HUBER_2D = np.float32(math.sqrt(5.99))       # BAoptimizer::thHuber2D
+HUBER_3D = np.float32(math.sqrt(7.815))      # BAoptimizer::thHuber3D
+
+
+@dataclasses.dataclass
+class Problem:
+    """A bundle-adjustment problem in the layout of the C-ABI bulk loader."""
+
+    cam_K: np.ndarray        # float32 [C, 4] fx fy cx cy
+    cam_bf: np.ndarray       # float32 [C]
+    cam_Tcb: np.ndarray      # float32 [C, 16] row-major T_cam_body
+    cam_size: np.ndarray     # int32 [C, 2] width height (generator metadata)
+    pose_Tcw: np.ndarray     # float32 [K, 16] row-major T_body_world
+    pose_fixed: np.ndarray   # uint8 [K]
+    point_Xw: np.ndarray     # float32 [P, 3]
+    point_fixed: np.ndarray  # uint8 [P]
+    edge_type: np.ndarray    # uint8 [E]
+    edge_pose: np.ndarray    # int32 [E]
+    edge_point: np.ndarray   # int32 [E]
+    edge_cam: np.ndarray     # int32 [E]
+    edge_obs: np.ndarray     # float32 [E, 3] u v u_right
+    edge_info: np.ndarray    # float32 [E]
+    edge_delta: np.ndarray   # float32 [E]
+    edge_robust: np.ndarray  # uint8 [E]
+    edge_level: np.ndarray   # uint8 [E]
+    gt_pose_Tcw: Optional[np.ndarray] = None  # float64 [K, 4, 4]
+    gt_point_Xw: Optional[np.ndarray] = None  # float64 [P, 3]
+    name: str = ""
+
+    @property
+    def n_cams(self) -> int:
+        return int(self.cam_K.shape[0])
+
+    @property
+    def n_poses(self) -> int:
+        return int(self.pose_Tcw.shape[0])
+
+    @property
+    def n_points(self) -> int:
+        return int(self.point_Xw.shape[0])
+
+    @property
+    def n_edges(self) -> int:
+        return int(self.edge_type.shape[0])
+
+    def copy(self) -> "Problem":
+        return dataclasses.replace(self, **{f.name: (getattr(self, f.name).copy()
+                                                      if isinstance(getattr(self, f.name), np.ndarray)
+                                                      else getattr(self, f.name))
+                                            for f in dataclasses.fields(self)})
+
+    def arrays(self) -> dict:
+        return {f.name: getattr(self, f.name) for f in dataclasses.fields(self)
+                if isinstance(getattr(self, f.name), np.ndarray)}
+
+    def save(self, path: str) -> None:
+        np.savez_compressed(path, name=np.array(self.name), **self.arrays())
+
+    @staticmethod
+    def load(path: str) -> "Problem":
+        z = np.load(path, allow_pickle=False)
+        kw = {k: z[k] for k in z.files if k != "name"}
+        for f in dataclasses.fields(Problem):
+            if f.name not in kw and f.name != "name":
+                kw[f.name] = None
+        return Problem(name=str(z["name"]) if "name" in z.files else "", **kw)
+
+
+# ----------------------------------------------------------------- geometry --
+def rot_y(a: float) -> np.ndarray:
+    c, s = math.cos(a), math.sin(a)
+    return np.array([[c, 0, s], [0, 1, 0], [-s, 0, c]])
+
+
+def so3_exp(w: np.ndarray) -> np.ndarray:
+    """Rodrigues' formula for a batch of rotation vectors [..., 3]."""
+    w = np.asarray(w, dtype=np.float64)
+    th = np.linalg.norm(w, axis=-1)[..., None, None]
+    K = np.zeros(w.shape[:-1] + (3, 3))
+    K[..., 0, 1] = -w[..., 2]
+    K[..., 0, 2] = w[..., 1]
+    K[..., 1, 0] = w[..., 2]
+    K[..., 1, 2] = -w[..., 0]
+    K[..., 2, 0] = -w[..., 1]
+    K[..., 2, 1] = w[..., 0]
+    small = th < 1e-12
+    ths = np.where(small, 1.0, th)
+    a = np.where(small, 1.0, np.sin(ths) / ths)
+    b = np.where(small, 0.5, (1 - np.cos(ths)) / (ths * ths))
+    return np.eye(3) + a * K + b * (K @ K)
+
+
+def make_T(R: np.ndarray, t: np.ndarray) -> np.ndarray:
+    T = np.zeros(R.shape[:-2] + (4, 4))
+    T[..., :3, :3] = R
+    T[..., :3, 3] = t
+    T[..., 3, 3] = 1.0
+    return T
+
+
+def inv_T(T: np.ndarray) -> np.ndarray:
+    R = T[..., :3, :3]
+    t = T[..., :3, 3]
+    Rt = np.swapaxes(R, -1, -2)
+    return make_T(Rt, -(Rt @ t[..., None])[..., 0])
+
+
+def random_rotations(rng: np.random.Generator, n: int) -> np.ndarray:
+    """Rotations uniform on SO(3) (normalised Gaussian quaternions)."""
+    q = rng.standard_normal((n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    x, y, z, w = q[:, 0], q[:, 1], q[:, 2], q[:, 3]
+    R = np.empty((n, 3, 3))
+    R[:, 0, 0] = 1 - 2 * (y * y + z * z)
+    R[:, 0, 1] = 2 * (x * y - z * w)
+    R[:, 0, 2] = 2 * (x * z + y * w)
+    R[:, 1, 0] = 2 * (x * y + z * w)
+    R[:, 1, 1] = 1 - 2 * (x * x + z * z)
+    R[:, 1, 2] = 2 * (y * z - x * w)
+    R[:, 2, 0] = 2 * (x * z - y * w)
+    R[:, 2, 1] = 2 * (y * z + x * w)
+    R[:, 2, 2] = 1 - 2 * (x * x + y * y)
+    return R
+
+
+# ---------------------------------------------------------------------- rig --
+@dataclasses.dataclass
+class Rig:
+    K: np.ndarray       # [C, 4] float32
+    size: np.ndarray    # [C, 2]
+    T_cb: np.ndarray    # [C, 4, 4] float64 T_cam_body
+    bf: np.ndarray      # [C] float32
+
+
+def baseline_rig(narrow_hfov_deg: float = 30.0, yaw_deg: float = 30.0) -> Rig:
+    """Left/right 640x480 at x=0 / x=1.0 m yawed outward, wide 1280x720 110 deg at x=0.5 m."""
+    fn = 320.0 / math.tan(math.radians(narrow_hfov_deg) / 2)
+    fw = 640.0 / math.tan(math.radians(110.0) / 2)
+    K = np.array([[fn, fn, 320.0, 240.0], [fn, fn, 320.0, 240.0], [fw, fw, 640.0, 360.0]], dtype=np.float32)
+    size = np.array([[640, 480], [640, 480], [1280, 720]], dtype=np.int32)
+    y = math.radians(yaw_deg)
+    T_bc = np.stack([make_T(rot_y(-y), np.array([0.0, 0, 0])),
+                     make_T(rot_y(+y), np.array([1.0, 0, 0])),
+                     make_T(np.eye(3), np.array([0.5, 0, 0]))])
+    bf = np.array([fn * 1.0, fn * 1.0, 0.0], dtype=np.float32)
+    return Rig(K=K, size=size, T_cb=inv_T(T_bc), bf=bf)
+
+
+def reference_rig() -> Rig:
+    """The reference's own rig: three 512x512 cameras (config/*.yaml), left = body."""
+    K = np.array([[955.40503, 955.40503, 256.0, 256.0],
+                  [955.40503, 955.40503, 256.0, 256.0],
+                  [179.25313, 179.25313, 256.0, 256.0]], dtype=np.float32)
+    size = np.array([[512, 512]] * 3, dtype=np.int32)
+    T_bc = np.stack([np.eye(4), make_T(np.eye(3), np.array([1.0, 0, 0])),
+                     make_T(np.eye(3), np.array([0.5, 0, 0]))])
+    bf = np.array([955.40503, 955.40503, 0.0], dtype=np.float32)
+    return Rig(K=K, size=size, T_cb=inv_T(T_bc), bf=bf)
+
+
+# --------------------------------------------------------------- trajectory --
+def drone_trajectory(rng: np.random.Generator, n: int, step: float = 0.3,
+                     max_rot_deg: float = 5.0) -> np.ndarray:
+    """World-from-body poses [n, 4, 4] of a smooth random drone path."""
+    T_wb = np.zeros((n, 4, 4))
+    R = np.eye(3)
+    p = np.zeros(3)
+    yaw_rate = 0.0
+    heading = np.array([0.0, 0.0, 1.0])
+    lim = math.radians(max_rot_deg)
+    for k in range(n):
+        T_wb[k] = make_T(R, p)
+        yaw_rate = float(np.clip(yaw_rate + rng.normal(0, math.radians(1.0)), -math.radians(4.0), math.radians(4.0)))
+        w = np.array([rng.normal(0, math.radians(0.5)), yaw_rate, rng.normal(0, math.radians(0.5))])
+        ang = np.linalg.norm(w)
+        if ang > lim:
+            w *= lim / ang
+        R = R @ so3_exp(w)
+        drift = rng.normal(0, 0.15, 3)
+        drift[1] *= 0.3
+        heading = 0.8 * heading + 0.2 * (R[:, 2] + drift)
+        heading /= np.linalg.norm(heading)
+        p = p + step * heading
+    return T_wb
+
+
+# ------------------------------------------------------------------ helpers --
+def _project(K: np.ndarray, Pc: np.ndarray) -> np.ndarray:
+    z = Pc[..., 2]
+    u = K[0] * Pc[..., 0] / z + K[2]
+    v = K[1] * Pc[..., 1] / z + K[3]
+    return np.stack([u, v], axis=-1)
+
+
+def _perturb_pose(rng, T_bw: np.ndarray, rot_deg: float, trans_m: float) -> np.ndarray:
+    T_wb = inv_T(T_bw)
+    dR = so3_exp(rng.normal(0, math.radians(rot_deg), 3))
+    T_wb2 = make_T(T_wb[:3, :3] @ dR, T_wb[:3, 3] + rng.normal(0, trans_m, 3))
+    return inv_T(T_wb2)
+
+
+def _finish(rig: Rig, T_bw_true, T_bw_init, pose_fixed, X_true, X_init, point_fixed,
+            e_pose, e_point, e_cam, obs, e_type=None, delta=HUBER_BENCH, name="") -> Problem:
+    E = len(e_pose)
+    if e_type is None:
+        e_type = np.zeros(E, np.uint8)
+    obs3 = np.zeros((E, 3), np.float32)
+    obs3[:, : obs.shape[1]] = obs
+    return Problem(
+        cam_K=rig.K.astype(np.float32), cam_bf=rig.bf.astype(np.float32),
+        cam_Tcb=rig.T_cb.astype(np.float32).reshape(-1, 16), cam_size=rig.size.astype(np.int32),
+        pose_Tcw=T_bw_init.astype(np.float32).reshape(-1, 16), pose_fixed=pose_fixed.astype(np.uint8),
+        point_Xw=X_init.astype(np.float32), point_fixed=point_fixed.astype(np.uint8),
+        edge_type=np.asarray(e_type, np.uint8), edge_pose=np.asarray(e_pose, np.int32),
+        edge_point=np.asarray(e_point, np.int32), edge_cam=np.asarray(e_cam, np.int32),
+        edge_obs=obs3, edge_info=np.ones(E, np.float32),
+        edge_delta=np.full(E, delta, np.float32), edge_robust=np.ones(E, np.uint8),
+        edge_level=np.zeros(E, np.uint8), gt_pose_Tcw=T_bw_true, gt_point_Xw=X_true, name=name)
+
+
+# ----------------------------------------------------------------- local BA --
+def local_ba(n_kf: int, n_points: int, seed: int, outlier_frac: float = 0.05,
+             n_fixed: int = 2, rig: Optional[Rig] = None, box_offset: float = 0.0,
+             max_obs: int = 8, corridor: bool = False, name: str = "") -> Problem:
+    """Local-BA window: n_kf keyframes x 3 cameras observing n_points map points."""
+    rng = np.random.default_rng(seed)
+    rig = rig or baseline_rig()
+    T_wb = drone_trajectory(rng, n_kf)
+    T_bw = inv_T(T_wb)
+    # box 20 (x) x 10 (y, vertical) x 20 (z) m, centred ahead of the mid trajectory
+    if corridor:
+        # large maps: each point lives in a 20 x 10 x 20 m box ahead of a
+        # random keyframe, so the map follows the whole trajectory
+        anchor = rng.integers(0, n_kf, n_points)
+        centre = T_wb[anchor, :3, 3] + T_wb[anchor, :3, 2] * (10.0 + box_offset)
+        X = centre + rng.uniform(-0.5, 0.5, (n_points, 3)) * np.array([20.0, 10.0, 20.0])
+    else:
+        # box 20 (x) x 10 (y, vertical) x 20 (z) m, centred ahead of the mid trajectory
+        mid = T_wb[n_kf // 2, :3, 3]
+        fwd = T_wb[n_kf // 2, :3, 2]
+        centre = mid + fwd * (10.0 + box_offset)
+        X = centre + rng.uniform(-0.5, 0.5, (n_points, 3)) * np.array([20.0, 10.0, 20.0])
+    # visibility of every point in every camera, one keyframe at a time
+    C = rig.K.shape[0]
+    T_cw = rig.T_cb[None, :, :, :] @ T_bw[:, None, :, :]          # [K, C, 4, 4]
+    vk_l, vc_l, vp_l, uv_l = [], [], [], []
+    for k in range(n_kf):
+        for c in range(C):
+            Pc = X @ T_cw[k, c, :3, :3].T + T_cw[k, c, :3, 3]
+            ok = Pc[:, 2] > 0.5
+            uv = _project(rig.K[c].astype(np.float64), Pc)
+            w, h = rig.size[c]
+            ok &= (uv[:, 0] >= 0) & (uv[:, 0] < w) & (uv[:, 1] >= 0) & (uv[:, 1] < h)
+            idx = np.nonzero(ok)[0]
+            vk_l.append(np.full(len(idx), k)); vc_l.append(np.full(len(idx), c))
+            vp_l.append(idx); uv_l.append(uv[idx])
+    vk = np.concatenate(vk_l); vc = np.concatenate(vc_l); vp = np.concatenate(vp_l)
+    uvall = np.concatenate(uv_l)
+    # per point: keep 2..max_obs observations (random subset when more)
+    order = np.lexsort((rng.random(len(vp)), vp))
+    vk, vc, vp, uvall = vk[order], vc[order], vp[order], uvall[order]
+    counts = np.bincount(vp, minlength=n_points)
+    starts = np.concatenate([[0], np.cumsum(counts)[:-1]])
+    rank = np.arange(len(vp)) - starts[vp]
+    keep = (rank < max_obs) & (counts[vp] >= 2)
+    vk, vc, vp, uvall = vk[keep], vc[keep], vp[keep], uvall[keep]
+    used = np.unique(vp)
+    remap = -np.ones(n_points, np.int64)
+    remap[used] = np.arange(len(used))
+    X = X[used]
+    vp = remap[vp]
+    # edges in keyframe-major order (the way PoseEstimation walks keyframes)
+    o = np.lexsort((vp, vc, vk))
+    vk, vc, vp, z = vk[o], vc[o], vp[o], uvall[o]
+    z = z + rng.normal(0, 1.0, z.shape)
+    out = rng.random(len(vk)) < outlier_frac
+    sz = rig.size[vc].astype(np.float64)
+    z[out] = rng.uniform(0, 1, (int(out.sum()), 2)) * sz[out]
+    # initial estimates
+    fixed = np.zeros(n_kf, np.uint8)
+    fixed[:n_fixed] = 1
+    T_init = T_bw.copy()
+    for k in range(n_fixed, n_kf):
+        T_init[k] = _perturb_pose(rng, T_bw[k], 1.0, 0.05)
+    X_init = X + rng.normal(0, 0.1, X.shape)
+    return _finish(rig, T_bw, T_init, fixed, X, X_init, np.zeros(len(X), np.uint8),
+                   vk, vp, vc, z, name=name or f"local_ba_{n_kf}kf_{n_points}pts")
+
+
+def reference_style(seed: int, n_kf: int = 5, n_points: int = 300) -> Problem:
+    """Small problem on the reference rig with all three edge kinds: stereo
+    edges (left observations with a right-image match, Huber sqrt(7.815)),
+    mono left edges (Huber sqrt(5.99)) and wide-camera edges to the body
+    (Huber sqrt(7.815)), some fixed points -- the mix BoundleAdjustment builds
+    (include/PoseEstimation.hpp:40-101)."""
+    rng = np.random.default_rng(seed)
+    rig = reference_rig()
+    T_wb = drone_trajectory(rng, n_kf)
+    T_bw = inv_T(T_wb)
+    mid = T_wb[n_kf // 2, :3, 3]
+    fwd = T_wb[n_kf // 2, :3, 2]
+    X = mid + fwd * 12.0 + rng.uniform(-0.5, 0.5, (n_points, 3)) * np.array([16.0, 8.0, 12.0])
+    ep, ex, ec, et, eo, ed = [], [], [], [], [], []
+    for k in range(n_kf):
+        for c in (0, 2):
+            T = rig.T_cb[c] @ T_bw[k]
+            Pc = X @ T[:3, :3].T + T[:3, 3]
+            uv = _project(rig.K[c].astype(np.float64), Pc)
+            w, h = rig.size[c]
+            ok = (Pc[:, 2] > 0.5) & (uv[:, 0] >= 0) & (uv[:, 0] < w) & (uv[:, 1] >= 0) & (uv[:, 1] < h)
+            for p in np.nonzero(ok)[0]:
+                u = uv[p] + rng.normal(0, 1.0, 2)
+                if c == 0:
+                    ur = u[0] - float(rig.bf[0]) / Pc[p, 2] + rng.normal(0, 1.0)
+                    stereo = rng.random() < 0.5 and (u[0] - ur) >= 1.0
+                    ep.append(k); ex.append(p); ec.append(0)
+                    et.append(EDGE_STEREO if stereo else EDGE_MONO)
+                    eo.append([u[0], u[1], ur if stereo else 0.0])
+                    ed.append(HUBER_3D if stereo else HUBER_2D)
+                else:
+                    ep.append(k); ex.append(p); ec.append(2); et.append(EDGE_MONO)
+                    eo.append([u[0], u[1], 0.0]); ed.append(HUBER_3D)
+    E = len(ep)
+    eo = np.asarray(eo)
+    out = rng.random(E) < 0.05
+    eo[out, 0] = rng.uniform(0, 512, out.sum())
+    eo[out, 1] = rng.uniform(0, 512, out.sum())
+    seen = np.bincount(np.asarray(ex), minlength=n_points)
+    fixed_pts = (rng.random(n_points) < 0.2).astype(np.uint8)
+    fixed = np.zeros(n_kf, np.uint8)
+    fixed[0] = 1
+    T_init = T_bw.copy()
+    for k in range(1, n_kf):
+        T_init[k] = _perturb_pose(rng, T_bw[k], 0.5, 0.03)
+    X_init = X + rng.normal(0, 0.05, X.shape) * (1 - fixed_pts[:, None])
+    pr = _finish(rig, T_bw, T_init, fixed, X, X_init, fixed_pts, ep, ex, ec, eo.astype(np.float32),
+                 e_type=et, name=f"reference_style_{seed}")
+    pr.edge_delta = np.asarray(ed, np.float32)
+    del seen
+    return pr
+
+
+# ---------------------------------------------------------------- pose-only --
+def pose_only(n_obs: int, seed: int, outlier_frac: float = 0.10, rig: Optional[Rig] = None,
+              delta=HUBER_BENCH) -> Problem:
+    """One frame with n_obs observations of fixed map points (Tracker's
+    pose-only optimisation, src/PoseEstimation.cpp:48-130): points sampled in
+    the three cameras' frusta at depth U(1, 30) m, 10% outliers, the body
+    pose perturbed N(0, 0.05 m / 1 deg)."""
+    rng = np.random.default_rng(seed)
+    rig = rig or baseline_rig()
+    R = random_rotations(rng, 1)[0]
+    T_wb = make_T(R, rng.normal(0, 5.0, 3))
+    T_bw = inv_T(T_wb)
+    cam = rng.integers(0, rig.K.shape[0], n_obs)
+    sz = rig.size[cam].astype(np.float64)
+    uv = rng.uniform(0, 1, (n_obs, 2)) * sz
+    d = rng.uniform(1.0, 30.0, n_obs)
+    K = rig.K[cam].astype(np.float64)
+    Pc = np.stack([(uv[:, 0] - K[:, 2]) / K[:, 0] * d, (uv[:, 1] - K[:, 3]) / K[:, 1] * d, d], axis=1)
+    T_wc = T_wb[None] @ inv_T(rig.T_cb)[cam]
+    X = np.einsum("nij,nj->ni", T_wc[:, :3, :3], Pc) + T_wc[:, :3, 3]
+    z = uv + rng.normal(0, 1.0, uv.shape)
+    out = rng.random(n_obs) < outlier_frac
+    z[out] = rng.uniform(0, 1, (int(out.sum()), 2)) * sz[out]
+    T_init = _perturb_pose(rng, T_bw, 1.0, 0.05)
+    return _finish(rig, T_bw[None], T_init[None], np.zeros(1, np.uint8), X, X,
+                   np.ones(n_obs, np.uint8), np.zeros(n_obs, np.int64), np.arange(n_obs), cam, z,
+                   delta=delta, name=f"pose_only_{n_obs}")
+
+
+# ------------------------------------------------------------ random edges --
+def random_edges(n: int, seed: int, rig: Optional[Rig] = None):
+    """Independent mono edges for the differentiation check: body poses with
+    rotations uniform on SO(3) and translations N(0, 5 m), the baseline rig's
+    extrinsics, points at depth U(1, 50) m in front of their camera.
+
+    Returns (T_bw [n,4,4] f64, T_cb [n,4,4] f64, K [n,4] f64, X [n,3] f64,
+    obs [n,2] f64, cam [n] int)."""
+    rng = np.random.default_rng(seed)
+    rig = rig or baseline_rig()
+    R = random_rotations(rng, n)
+    T_wb = make_T(R, rng.normal(0, 5.0, (n, 3)))
+    cam = rng.integers(0, rig.K.shape[0], n)
+    K = rig.K[cam].astype(np.float64)
+    sz = rig.size[cam].astype(np.float64)
+    uv = rng.uniform(0, 1, (n, 2)) * sz
+    d = rng.uniform(1.0, 50.0, n)
+    Pc = np.stack([(uv[:, 0] - K[:, 2]) / K[:, 0] * d, (uv[:, 1] - K[:, 3]) / K[:, 1] * d, d], axis=1)
+    T_wc = T_wb @ inv_T(rig.T_cb)[cam]
+    X = np.einsum("nij,nj->ni", T_wc[:, :3, :3], Pc) + T_wc[:, :3, 3]
+    obs = uv + rng.normal(0, 1.0, uv.shape)
+    return inv_T(T_wb), rig.T_cb[cam], K, X, obs, cam
+
+
+# ------------------------------------------------------------ named configs --
+def config(idx: int, rep: int = 0) -> Problem:
+    """Benchmark configurations (1-based, seed = idx * 1000 + rep).
+
+    1: 10 keyframes, 2000 points (~9k edges); 2: 30 keyframes, 20k points
+    (~150k observations); 5: 300 keyframes, 200k points (~2M observations)."""
+    seed = idx * 1000 + rep
+    if idx == 1:
+        return local_ba(10, 2000, seed, box_offset=CONFIG_BOX_OFFSET[1], name="config1_10kf_2000pts")
+    if idx == 2:
+        return local_ba(30, 20000, seed, box_offset=CONFIG_BOX_OFFSET[2], name="config2_30kf_20kpts")
+    if idx == 5:
+        return local_ba(300, 200000, seed, box_offset=CONFIG_BOX_OFFSET[5], corridor=True,
+                        name="config5_300kf_200kpts")
+    raise ValueError(f"config {idx} is not a single local-BA problem")
+
+
+# box placement that gives the configurations' edge counts (~9k / ~150k / ~2M)
+CONFIG_BOX_OFFSET = {1: -4.0, 2: 0.0, 5: 0.0}

@@ -1,0 +1,245 @@
+"""ctypes front end of the CPU oracle -- TEST INFRASTRUCTURE, NOT PRODUCT CODE.
+
+Only the tests, the smoke check and the benchmark's CPU legs import this
+module; the product path never does.  Parity status: unpinned (the
+reference has no golden vectors and cannot be built here); see the header
+of g2o_oracle.cpp for what the restatement follows.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from oracle import build_oracle
+
+_LIBS: dict = {}
+
+c_float_p = ctypes.POINTER(ctypes.c_float)
+c_double_p = ctypes.POINTER(ctypes.c_double)
+c_u8_p = ctypes.POINTER(ctypes.c_uint8)
+c_i32_p = ctypes.POINTER(ctypes.c_int32)
+
+
+class OrcProblem(ctypes.Structure):
+    _fields_ = [
+        ("n_cams", ctypes.c_int32), ("cam_K", c_float_p), ("cam_bf", c_float_p), ("cam_Tcb", c_float_p),
+        ("n_poses", ctypes.c_int32), ("pose_Tcw", c_float_p), ("pose_fixed", c_u8_p),
+        ("n_points", ctypes.c_int32), ("point_Xw", c_float_p), ("point_fixed", c_u8_p),
+        ("n_edges", ctypes.c_int32), ("edge_type", c_u8_p), ("edge_pose", c_i32_p),
+        ("edge_point", c_i32_p), ("edge_cam", c_i32_p), ("edge_obs", c_float_p),
+        ("edge_info", c_float_p), ("edge_delta", c_float_p), ("edge_robust", c_u8_p),
+        ("edge_level", c_u8_p),
+    ]
+
+
+class OrcTrialLog(ctypes.Structure):
+    _fields_ = [
+        ("iteration", ctypes.c_int32), ("trial", ctypes.c_int32), ("chi_before", ctypes.c_double),
+        ("chi_after", ctypes.c_double), ("lambda_", ctypes.c_double), ("scale", ctypes.c_double),
+        ("rho", ctypes.c_double), ("accepted", ctypes.c_int32), ("solve_ok", ctypes.c_int32),
+    ]
+
+
+class OrcResult(ctypes.Structure):
+    _fields_ = [
+        ("pose_qt", c_double_p), ("pose_Tcw", c_float_p), ("point_X", c_double_p),
+        ("edge_chi2", c_double_p), ("edge_level", c_u8_p), ("log", ctypes.POINTER(OrcTrialLog)),
+        ("log_cap", ctypes.c_int32), ("n_log", ctypes.c_int32), ("iterations_done", ctypes.c_int32),
+        ("n_active_edges", ctypes.c_int32), ("final_chi2", ctypes.c_double),
+        ("seconds_linearize", ctypes.c_double), ("seconds_total", ctypes.c_double),
+        ("edges_linearized", ctypes.c_int64),
+    ]
+
+
+LOG_DTYPE = np.dtype([("iteration", np.int32), ("trial", np.int32), ("chi_before", np.float64),
+                      ("chi_after", np.float64), ("lambda", np.float64), ("scale", np.float64),
+                      ("rho", np.float64), ("accepted", np.int32), ("solve_ok", np.int32)], align=True)
+
+
+def lib(threads: bool = False):
+    name = "liboracle_omp.so" if threads else "liboracle.so"
+    if name not in _LIBS:
+        paths = build_oracle.build()
+        L = ctypes.CDLL(paths[name])
+        L.orc_optimize.argtypes = [ctypes.POINTER(OrcProblem), ctypes.c_int, ctypes.c_int, ctypes.POINTER(OrcResult)]
+        L.orc_pose_optimization.argtypes = [ctypes.POINTER(OrcProblem), ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                            ctypes.c_int, ctypes.c_int, ctypes.POINTER(OrcResult),
+                                            ctypes.POINTER(ctypes.c_int)]
+        L.orc_local_ba.argtypes = [ctypes.POINTER(OrcProblem), ctypes.c_int, ctypes.c_float, ctypes.c_int,
+                                   ctypes.POINTER(OrcResult), ctypes.POINTER(ctypes.c_int)]
+        L.orc_linearize_edges.argtypes = [ctypes.POINTER(OrcProblem), c_double_p, c_double_p, c_double_p]
+        L.orc_normal_equations.argtypes = [ctypes.POINTER(OrcProblem), ctypes.c_double, c_double_p, c_double_p,
+                                           c_double_p, ctypes.c_int]
+        for fn in ("orc_se3_exp", "orc_mat44f_to_qt", "orc_qt_to_mat44f", "orc_huber", "orc_compose", "orc_map"):
+            getattr(L, fn).restype = None
+        _LIBS[name] = L
+    return _LIBS[name]
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(t) if a is not None else None
+
+
+def problem_struct(pr):
+    """Pack a mcvslam_gb300.synth.Problem into the C struct; returns (struct, keepalive)."""
+    keep = {}
+
+    def arr(name, dt, shape_last=None):
+        a = np.ascontiguousarray(getattr(pr, name), dtype=dt)
+        keep[name] = a
+        return a
+
+    s = OrcProblem()
+    s.n_cams = pr.n_cams
+    s.cam_K = _ptr(arr("cam_K", np.float32), c_float_p)
+    s.cam_bf = _ptr(arr("cam_bf", np.float32), c_float_p)
+    s.cam_Tcb = _ptr(arr("cam_Tcb", np.float32), c_float_p)
+    s.n_poses = pr.n_poses
+    s.pose_Tcw = _ptr(arr("pose_Tcw", np.float32), c_float_p)
+    s.pose_fixed = _ptr(arr("pose_fixed", np.uint8), c_u8_p)
+    s.n_points = pr.n_points
+    s.point_Xw = _ptr(arr("point_Xw", np.float32), c_float_p)
+    s.point_fixed = _ptr(arr("point_fixed", np.uint8), c_u8_p)
+    s.n_edges = pr.n_edges
+    s.edge_type = _ptr(arr("edge_type", np.uint8), c_u8_p)
+    s.edge_pose = _ptr(arr("edge_pose", np.int32), c_i32_p)
+    s.edge_point = _ptr(arr("edge_point", np.int32), c_i32_p)
+    s.edge_cam = _ptr(arr("edge_cam", np.int32), c_i32_p)
+    s.edge_obs = _ptr(arr("edge_obs", np.float32), c_float_p)
+    s.edge_info = _ptr(arr("edge_info", np.float32), c_float_p)
+    s.edge_delta = _ptr(arr("edge_delta", np.float32), c_float_p)
+    s.edge_robust = _ptr(arr("edge_robust", np.uint8), c_u8_p)
+    s.edge_level = _ptr(arr("edge_level", np.uint8), c_u8_p)
+    return s, keep
+
+
+def _result(pr, log_cap):
+    out = {
+        "pose_qt": np.zeros((pr.n_poses, 7)),
+        "pose_Tcw": np.zeros((pr.n_poses, 16), np.float32),
+        "point_X": np.zeros((pr.n_points, 3)),
+        "edge_chi2": np.zeros(pr.n_edges),
+        "edge_level": np.zeros(pr.n_edges, np.uint8),
+        "log": np.zeros(log_cap, LOG_DTYPE),
+    }
+    r = OrcResult()
+    r.pose_qt = _ptr(out["pose_qt"], c_double_p)
+    r.pose_Tcw = _ptr(out["pose_Tcw"], c_float_p)
+    r.point_X = _ptr(out["point_X"], c_double_p)
+    r.edge_chi2 = _ptr(out["edge_chi2"], c_double_p)
+    r.edge_level = _ptr(out["edge_level"], c_u8_p)
+    r.log = out["log"].ctypes.data_as(ctypes.POINTER(OrcTrialLog))
+    r.log_cap = log_cap
+    return r, out
+
+
+def _finish(r, out):
+    out["log"] = out["log"][: min(r.n_log, r.log_cap)].copy()
+    out["iterations_done"] = r.iterations_done
+    out["n_active_edges"] = r.n_active_edges
+    out["final_chi2"] = r.final_chi2
+    out["seconds_linearize"] = r.seconds_linearize
+    out["seconds_total"] = r.seconds_total
+    out["edges_linearized"] = r.edges_linearized
+    return out
+
+
+def optimize(pr, iterations: int, n_threads: int = 1, log_cap: int = 4096) -> dict:
+    s, keep = problem_struct(pr)
+    r, out = _result(pr, log_cap)
+    ret = lib(n_threads > 1).orc_optimize(ctypes.byref(s), iterations, n_threads, ctypes.byref(r))
+    out = _finish(r, out)
+    out["ret"] = ret
+    return out
+
+
+def pose_optimization(pr, rounds: int = 4, iters: int = 15, chi2_thr: float = 5.991,
+                      drop_robust_round: int = 2, n_threads: int = 1, log_cap: int = 4096) -> dict:
+    s, keep = problem_struct(pr)
+    r, out = _result(pr, log_cap)
+    written = ctypes.c_int(0)
+    ret = lib(n_threads > 1).orc_pose_optimization(ctypes.byref(s), rounds, iters, chi2_thr, drop_robust_round,
+                                                   n_threads, ctypes.byref(r), ctypes.byref(written))
+    out = _finish(r, out)
+    out["ret"] = ret
+    out["pose_written"] = written.value
+    return out
+
+
+def local_ba(pr, iterations: int = 10, chi2_thr: float = 5.991, n_threads: int = 1, log_cap: int = 4096) -> dict:
+    s, keep = problem_struct(pr)
+    r, out = _result(pr, log_cap)
+    written = ctypes.c_int(0)
+    ret = lib(n_threads > 1).orc_local_ba(ctypes.byref(s), iterations, chi2_thr, n_threads, ctypes.byref(r),
+                                          ctypes.byref(written))
+    out = _finish(r, out)
+    out["ret"] = ret
+    out["written"] = written.value
+    return out
+
+
+def linearize_edges(pr):
+    s, keep = problem_struct(pr)
+    E = pr.n_edges
+    err = np.zeros((E, 3))
+    Jl = np.zeros((E, 3, 3))
+    Jp = np.zeros((E, 3, 6))
+    lib().orc_linearize_edges(ctypes.byref(s), _ptr(err, c_double_p), _ptr(Jl, c_double_p), _ptr(Jp, c_double_p))
+    return err, Jl, Jp
+
+
+def normal_equations(pr, lam: float, cap: int = 4000):
+    s, keep = problem_struct(pr)
+    H = np.zeros(cap * cap)
+    b = np.zeros(cap)
+    x = np.zeros(cap)
+    N = lib().orc_normal_equations(ctypes.byref(s), lam, _ptr(H, c_double_p), _ptr(b, c_double_p),
+                                   _ptr(x, c_double_p), cap)
+    if N <= 0:
+        raise ValueError(f"normal equations too large or empty ({N})")
+    return H[: N * N].reshape(N, N), b[:N], x[:N]
+
+
+def se3_exp(u) -> np.ndarray:
+    u = np.ascontiguousarray(u, np.float64)
+    o = np.zeros(7)
+    lib().orc_se3_exp(_ptr(u, c_double_p), _ptr(o, c_double_p))
+    return o
+
+
+def mat44f_to_qt(T) -> np.ndarray:
+    T = np.ascontiguousarray(T, np.float32).reshape(16)
+    o = np.zeros(7)
+    lib().orc_mat44f_to_qt(_ptr(T, c_float_p), _ptr(o, c_double_p))
+    return o
+
+
+def qt_to_mat44f(qt) -> np.ndarray:
+    qt = np.ascontiguousarray(qt, np.float64)
+    o = np.zeros(16, np.float32)
+    lib().orc_qt_to_mat44f(_ptr(qt, c_double_p), _ptr(o, c_float_p))
+    return o.reshape(4, 4)
+
+
+def huber(e2: float, delta: float) -> np.ndarray:
+    o = np.zeros(3)
+    lib().orc_huber(ctypes.c_double(e2), ctypes.c_double(delta), _ptr(o, c_double_p))
+    return o
+
+
+def compose(a, b) -> np.ndarray:
+    a = np.ascontiguousarray(a, np.float64)
+    b = np.ascontiguousarray(b, np.float64)
+    o = np.zeros(7)
+    lib().orc_compose(_ptr(a, c_double_p), _ptr(b, c_double_p), _ptr(o, c_double_p))
+    return o
+
+
+def map_point(qt, X) -> np.ndarray:
+    qt = np.ascontiguousarray(qt, np.float64)
+    X = np.ascontiguousarray(X, np.float64)
+    o = np.zeros(3)
+    lib().orc_map(_ptr(qt, c_double_p), _ptr(X, c_double_p), _ptr(o, c_double_p))
+    return o

@@ -1,0 +1,153 @@
+"""GPU solver vs the CPU oracle through the C ABI.
+
+FP64 plain mode must follow g2o's LM trial by trial: chi2 within 1e-9
+relative, the same accept/reject decisions and lambda sequence, final poses
+within 1e-8 m / 1e-8 rad.  Mixed precision must end within 1e-6 relative of
+the FP64 final cost (evaluated in FP64)."""
+import numpy as np
+import pytest
+
+from mcvslam_gb300 import ba, synth
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+CHI_RTOL = 1e-9
+POSE_TOL_M = 1e-8
+POSE_TOL_RAD = 1e-8
+
+
+def rot_diff(qa, qb):
+    """Angle (rad) between two unit quaternions (x y z w)."""
+    d = abs(float(np.dot(qa, qb)))
+    c = np.linalg.norm(qa * 0 + np.array([
+        qa[3] * -qb[0] + qa[0] * qb[3] + qa[1] * -qb[2] - qa[2] * -qb[1],
+        qa[3] * -qb[1] + qa[1] * qb[3] + qa[2] * -qb[0] - qa[0] * -qb[2],
+        qa[3] * -qb[2] + qa[2] * qb[3] + qa[0] * -qb[1] - qa[1] * -qb[0]]))
+    return 2 * np.arctan2(c, d)
+
+
+def compare_logs(g, o):
+    assert len(g) == len(o), (len(g), len(o))
+    for a, b in zip(g, o):
+        assert (a["iteration"], a["trial"], a["accepted"], a["solve_ok"]) == \
+               (b["iteration"], b["trial"], b["accepted"], b["solve_ok"])
+        for k in ("chi_before", "chi_after", "lambda", "scale"):
+            assert abs(a[k] - b[k]) <= CHI_RTOL * abs(b[k]), (k, a, b)
+
+
+def compare_state(g, o, pr, pt_tol=1e-7):
+    qt, X = g["pose_qt"], g["point_X"]
+    for k in range(pr.n_poses):
+        assert np.abs(qt[k, 4:] - o["pose_qt"][k, 4:]).max() <= POSE_TOL_M
+        assert rot_diff(qt[k, :4], o["pose_qt"][k, :4]) <= POSE_TOL_RAD
+    assert np.abs(X - o["point_X"]).max() <= pt_tol
+
+
+@pytest.mark.parametrize("cfg", [1, 2])
+def test_fp64_follows_oracle_trial_by_trial(cfg, gpu):
+    pr = synth.config(cfg)
+    o = oracle.optimize(pr, 10)
+    g = ba.solve(pr, 10, "fp64")
+    assert g["stats"]["iterations"] == o["ret"]
+    compare_logs(g["log"], o["log"])
+    assert abs(g["stats"]["final_chi2"] - o["final_chi2"]) <= CHI_RTOL * o["final_chi2"]
+    compare_state(g, o, pr)
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_reference_style_stereo_and_fixed_points(seed, gpu):
+    pr = synth.reference_style(seed)
+    assert (pr.edge_type == 1).any() and pr.point_fixed.any()
+    o = oracle.optimize(pr, 10)
+    g = ba.solve(pr, 10, "fp64")
+    compare_logs(g["log"], o["log"])
+    compare_state(g, o, pr)
+
+
+def test_edge_chi2_matches_oracle(gpu):
+    pr = synth.reference_style(7)
+    o = oracle.optimize(pr, 5)
+    with ba.Solver() as s:
+        s.load(pr)
+        s.optimize(5)
+        chi2 = s.edge_chi2()
+    np.testing.assert_allclose(chi2, o["edge_chi2"], rtol=1e-8, atol=1e-9)
+
+
+def test_pose_only_rounds_match_oracle(gpu):
+    pr = synth.pose_only(800, seed=41)
+    o = oracle.pose_optimization(pr, rounds=4, iters=10, chi2_thr=5.991)
+    with ba.Solver() as s:
+        s.load(pr)
+        inl, written = s.pose_optimization(4, 10, 5.991, 2)
+        lv = s.levels()
+        qt, _ = s.state()
+    assert inl == o["ret"] and written == o["pose_written"]
+    np.testing.assert_array_equal(lv, o["edge_level"])
+    assert np.abs(qt[0, 4:] - o["pose_qt"][0, 4:]).max() <= POSE_TOL_M
+    assert rot_diff(qt[0, :4], o["pose_qt"][0, :4]) <= POSE_TOL_RAD
+
+
+def test_local_ba_filter_matches_oracle(gpu):
+    pr = synth.config(1)
+    o = oracle.local_ba(pr, 10)
+    with ba.Solver() as s:
+        s.load(pr)
+        succ, written = s.local_ba(10, 5.991)
+        lv = s.levels()
+    assert succ == o["ret"] and written == o["written"]
+    np.testing.assert_array_equal(lv, o["edge_level"])
+
+
+@pytest.mark.parametrize("cfg", [1, 2])
+def test_mixed_precision_final_cost_gap(cfg, gpu):
+    pr = synth.config(cfg)
+    plain = ba.solve(pr, 10, "fp64")
+    mixed = ba.solve(pr, 10, "mixed")
+    # FP64 cost of the mixed-precision result
+    with ba.Solver() as s:
+        s.load(pr)
+        s.set_state(mixed["pose_qt"], mixed["point_X"])
+        st = s.optimize(0)
+    chi_mixed = st["initial_chi2"]
+    chi_plain = plain["stats"]["final_chi2"]
+    gap = (chi_mixed - chi_plain) / chi_plain
+    assert gap <= 1e-6, gap
+    terr = np.abs(mixed["pose_qt"][:, 4:] - plain["pose_qt"][:, 4:]).max()
+    assert terr < 1e-3
+
+
+def test_solves_are_deterministic(gpu):
+    pr = synth.config(1)
+    a = ba.solve(pr, 10, "fp64")
+    b = ba.solve(pr, 10, "fp64")
+    np.testing.assert_array_equal(a["pose_qt"], b["pose_qt"])
+    np.testing.assert_array_equal(a["point_X"], b["point_X"])
+
+
+def test_points_only_problem(gpu):
+    pr = synth.config(1)
+    pr.pose_fixed[:] = 1
+    o = oracle.optimize(pr, 5)
+    g = ba.solve(pr, 5, "fp64")
+    compare_logs(g["log"], o["log"])
+    assert np.abs(g["point_X"] - o["point_X"]).max() <= 1e-8
+
+
+def test_poses_only_problem(gpu):
+    pr = synth.config(1)
+    pr.point_fixed[:] = 1
+    o = oracle.optimize(pr, 5)
+    g = ba.solve(pr, 5, "fp64")
+    compare_logs(g["log"], o["log"])
+    compare_state(g, o, pr)
+
+
+def test_zero_iterations_returns_initial_cost(gpu):
+    pr = synth.config(1)
+    with ba.Solver() as s:
+        s.load(pr)
+        st = s.optimize(0)
+    o = oracle.optimize(pr, 1)
+    assert abs(st["initial_chi2"] - o["log"][0]["chi_before"]) <= CHI_RTOL * o["log"][0]["chi_before"]
