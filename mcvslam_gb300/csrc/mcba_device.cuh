@@ -354,6 +354,78 @@ __device__ __forceinline__ void edge_jac(const EdgeRec& r, const StateView& v, c
 }
 
 // ------------------------------------------------------ reductions --
+// Accumulator of the linearisation real type.  FP64: a plain double.  FP32:
+// a float-float pair updated with Knuth's TwoSum, so that long FP32 sums
+// (thousands of edges per pose, of pairs per reduced-camera block) keep the
+// information that cancels in the Schur complement; all arithmetic stays FP32.
+template <typename R>
+struct Acc;
+template <>
+struct Acc<double> {
+  double v;
+  __device__ __forceinline__ void zero() { v = 0.0; }
+  __device__ __forceinline__ void add(double x) { v += x; }
+  __device__ __forceinline__ void add(const Acc& o) { v += o.v; }
+  __device__ __forceinline__ double value() const { return v; }
+  __device__ __forceinline__ Acc shfl_xor(int m) const {
+    Acc r;
+    r.v = __shfl_xor_sync(0xffffffffu, v, m);
+    return r;
+  }
+};
+template <>
+struct Acc<float> {
+  float hi, lo;
+  __device__ __forceinline__ void zero() { hi = lo = 0.f; }
+  __device__ __forceinline__ void add(float x) {
+    const float s = __fadd_rn(hi, x);
+    const float bb = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+    hi = s;
+    lo = __fadd_rn(lo, err);
+  }
+  __device__ __forceinline__ void add(const Acc& o) {
+    const float s = __fadd_rn(hi, o.hi);
+    const float bb = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(o.hi, bb));
+    hi = s;
+    lo = __fadd_rn(__fadd_rn(lo, o.lo), err);
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+  __device__ __forceinline__ Acc shfl_xor(int m) const {
+    Acc r;
+    r.hi = __shfl_xor_sync(0xffffffffu, hi, m);
+    r.lo = __shfl_xor_sync(0xffffffffu, lo, m);
+    return r;
+  }
+};
+
+// Reduce-scatter of 32 per-lane accumulators: afterwards lane l holds the
+// warp sum of slot l (recursive halving, 31 exchanges per lane).
+template <typename A>
+__device__ __forceinline__ A warp_reduce_scatter32_acc(A (&v)[32]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int s = 16; s >= 1; s >>= 1) {
+    const bool upper = (lane & s) != 0;
+#pragma unroll
+    for (int i = 0; i < s; ++i) {
+      const A send = upper ? v[i] : v[i + s];
+      A keep = upper ? v[i + s] : v[i];
+      keep.add(send.shfl_xor(s));
+      v[i] = keep;
+    }
+  }
+  return v[0];
+}
+
+template <typename A>
+__device__ __forceinline__ A warp_sum_acc(A x) {
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) x.add(x.shfl_xor(o));
+  return x;
+}
+
 // Reduce-scatter of 32 per-lane values: afterwards lane l holds the warp sum
 // of slot l (recursive halving, 31 shuffles per lane).
 template <typename T>

@@ -55,7 +55,8 @@ struct LMState {
   double lambda, ni, current_chi, temp_chi, rho, scale, initial_chi;
   int iteration, trial, cur, solve_ok;
   int trial_continue, terminate, total_trials, n_log;
-  int max_trials, max_log, last_accepted, pad;
+  int max_trials, max_log, last_accepted, max_iters;
+  int outer_runs, pad0;
 };
 
 struct Bufs {
@@ -86,13 +87,15 @@ struct Bufs {
   int* free_point_ids;
   // numeric workspaces (R-typed, stored as bytes)
   void* rows;       // [Ec][kRow]
-  void* partials;   // [nchunk][32]
-  void* Hpp;        // [Kf][36]
+  void* partials;   // [nchunk][32] accumulators
+  double* Hpp;      // [Kf][36] FP64 (formed from the accumulators)
   void* Hll;        // [Lf][6]
-  void* b;          // [6Kf + 3Lf]
+  double* bp;       // [6Kf] FP64
+  void* bl;         // [3Lf]
   void* yq;         // [Ec][kYQ]
-  void* ppart;      // [npchunk][36]
+  void* ppart;      // [npchunk][36] accumulators
   double* S;        // [(ld+32) x ld]
+  double* dinv;     // [ld] reciprocal Cholesky diagonal
   double* x;        // [6Kf + 3Lf]
   double* cost_part;
   double* scale_part;
@@ -153,9 +156,9 @@ __global__ void __launch_bounds__(kLinThreads) k_linearize(Bufs B) {
   const int ph = B.chunk_pose[c];
   const int j = jb + threadIdx.x;
   const StateView v = make_view(B, B.lm->cur);
-  R acc[32];
+  Acc<R> acc[32];
 #pragma unroll
-  for (int k = 0; k < 32; ++k) acc[k] = R(0);
+  for (int k = 0; k < 32; ++k) acc[k].zero();
   if (j < je) {
     const EdgeRec r = B.recs[j];
     const float obs[3] = {B.obs[3 * (size_t)j], B.obs[3 * (size_t)j + 1], B.obs[3 * (size_t)j + 2]};
@@ -214,49 +217,53 @@ __global__ void __launch_bounds__(kLinThreads) k_linearize(Bufs B) {
         for (int q = i; q < 6; ++q) {
           R h = wJp[0][i] * Jp[0][q] + wJp[1][i] * Jp[1][q];
           if (d3) h += wJp[2][i] * Jp[2][q];
-          acc[u6(i, q)] = h;
+          acc[u6(i, q)].add(h);
         }
         R bb = Jp[0][i] * om[0] + Jp[1][i] * om[1];
         if (d3) bb += Jp[2][i] * om[2];
-        acc[21 + i] = bb;
+        acc[21 + i].add(bb);
       }
     }
   }
   if (ph >= 0) {
-    __shared__ R sh[kLinThreads / 32][32];
-    const R mine = warp_reduce_scatter32(acc);
+    __shared__ Acc<R> sh[kLinThreads / 32][32];
+    const Acc<R> mine = warp_reduce_scatter32_acc(acc);
     sh[threadIdx.x >> 5][threadIdx.x & 31] = mine;
     __syncthreads();
     if (threadIdx.x < 32) {
-      R t = R(0);
+      Acc<R> t = sh[0][threadIdx.x];
 #pragma unroll
-      for (int w = 0; w < kLinThreads / 32; ++w) t += sh[w][threadIdx.x];
-      Ptrs<R>::p(B.partials)[(size_t)c * 32 + threadIdx.x] = t;
+      for (int w = 1; w < kLinThreads / 32; ++w) t.add(sh[w][threadIdx.x]);
+      reinterpret_cast<Acc<R>*>(B.partials)[(size_t)c * 32 + threadIdx.x] = t;
     }
   }
 }
 
-// Hpp / b_p: sum of the chunk partials of each free pose (warp per pose).
+// Hpp / b_p: sum of the chunk partials of each free pose (warp per pose),
+// stored in FP64.
 template <typename R>
 __global__ void k_pose_reduce(Bufs B, int Kf) {
   const int i = blockIdx.x;
   const int lane = threadIdx.x;
   if (i >= Kf) return;
   const int c0 = B.pose_chunk_begin[i], c1 = B.pose_chunk_begin[i + 1];
-  R s = R(0);
-  for (int c = c0; c < c1; ++c) s += Ptrs<R>::p(B.partials)[(size_t)c * 32 + lane];
-  R* H = Ptrs<R>::p(B.Hpp) + (size_t)i * 36;
+  const Acc<R>* part = reinterpret_cast<const Acc<R>*>(B.partials);
+  Acc<R> a;
+  a.zero();
+  for (int c = c0; c < c1; ++c) a.add(part[(size_t)c * 32 + lane]);
+  const double s = a.value();
+  double* H = B.Hpp + (size_t)i * 36;
   if (lane < 21) {
-    int a = 0, rem = lane;
-    while (rem >= 6 - a) {
-      rem -= 6 - a;
-      ++a;
+    int r = 0, rem = lane;
+    while (rem >= 6 - r) {
+      rem -= 6 - r;
+      ++r;
     }
-    const int bcol = a + rem;
-    H[a * 6 + bcol] = s;
-    H[bcol * 6 + a] = s;
+    const int bcol = r + rem;
+    H[r * 6 + bcol] = s;
+    H[bcol * 6 + r] = s;
   } else if (lane < 27) {
-    Ptrs<R>::p(B.b)[6 * (size_t)i + (lane - 21)] = s;
+    B.bp[6 * (size_t)i + (lane - 21)] = s;
   }
 }
 
@@ -277,7 +284,7 @@ __global__ void k_point_reduce(Bufs B, int Lf, int n) {
   R* H = Ptrs<R>::p(B.Hll) + (size_t)l * 6;
 #pragma unroll
   for (int k = 0; k < 6; ++k) H[k] = s[k];
-  R* b = Ptrs<R>::p(B.b) + n + 3 * (size_t)l;
+  R* b = Ptrs<R>::p(B.bl) + 3 * (size_t)l;
 #pragma unroll
   for (int k = 0; k < 3; ++k) b[k] = s[6 + k];
 }
@@ -287,9 +294,10 @@ __global__ void k_point_reduce(Bufs B, int Lf, int n) {
 template <typename R>
 __global__ void k_lambda_init(Bufs B, int Kf, int Lf, double tau) {
   __shared__ double sh[32];
+  if (B.lm->iteration != 0) return;
   double m = 0;
   for (int i = threadIdx.x; i < 6 * Kf; i += blockDim.x)
-    m = fmax(m, fabs((double)Ptrs<R>::p(B.Hpp)[(size_t)(i / 6) * 36 + 7 * (i % 6)]));
+    m = fmax(m, fabs(B.Hpp[(size_t)(i / 6) * 36 + 7 * (i % 6)]));
   for (int i = threadIdx.x; i < 3 * Lf; i += blockDim.x) {
     const int d = i % 3;
     m = fmax(m, fabs((double)Ptrs<R>::p(B.Hll)[(size_t)(i / 3) * 6 + (d == 0 ? 0 : d == 1 ? 3 : 5)]));
@@ -336,7 +344,7 @@ __global__ void k_schur_edge(Bufs B, int Ec, int n) {
   const R lam = (R)B.lm->lambda;
   R Di[9];
   damped_inverse<R>(Ptrs<R>::p(B.Hll) + (size_t)l * 6, lam, Di);
-  const R* bl = Ptrs<R>::p(B.b) + n + 3 * (size_t)l;
+  const R* bl = Ptrs<R>::p(B.bl) + 3 * (size_t)l;
   R db[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) db[i] = Di[3 * i] * bl[0] + Di[3 * i + 1] * bl[1] + Di[3 * i + 2] * bl[2];
@@ -362,11 +370,11 @@ __global__ void __launch_bounds__(256) k_schur_pairs(Bufs B, int npc) {
   const int lane = threadIdx.x & 31;
   if (warp >= npc) return;
   const int p0 = B.pchunk_begin[warp], p1 = B.pchunk_begin[warp + 1];
-  R acc[32], acc2[4];
+  Acc<R> acc[32], acc2[4];
 #pragma unroll
-  for (int k = 0; k < 32; ++k) acc[k] = R(0);
+  for (int k = 0; k < 32; ++k) acc[k].zero();
 #pragma unroll
-  for (int k = 0; k < 4; ++k) acc2[k] = R(0);
+  for (int k = 0; k < 4; ++k) acc2[k].zero();
   const R* yq = Ptrs<R>::p(B.yq);
   const R* rows = Ptrs<R>::p(B.rows);
   for (int p = p0 + lane; p < p1; p += 32) {
@@ -386,17 +394,17 @@ __global__ void __launch_bounds__(256) k_schur_pairs(Bufs B, int npc) {
         const R v = y[r * 3] * h[c * 3] + y[r * 3 + 1] * h[c * 3 + 1] + y[r * 3 + 2] * h[c * 3 + 2];
         const int t = r * 6 + c;
         if (t < 32)
-          acc[t] += v;
+          acc[t].add(v);
         else
-          acc2[t - 32] += v;
+          acc2[t - 32].add(v);
       }
   }
-  const R mine = warp_reduce_scatter32(acc);
-  R* out = Ptrs<R>::p(B.ppart) + (size_t)warp * 36;
+  const Acc<R> mine = warp_reduce_scatter32_acc(acc);
+  Acc<R>* out = reinterpret_cast<Acc<R>*>(B.ppart) + (size_t)warp * 36;
   out[lane] = mine;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    const R s = warp_sum(acc2[k]);
+    const Acc<R> s = warp_sum_acc(acc2[k]);
     if (lane == 0) out[32 + k] = s;
   }
 }
@@ -411,16 +419,17 @@ __global__ void k_schur_assemble(Bufs B, int ld) {
   if (t >= 36) return;
   const int a = B.block_ab[2 * blk], bb = B.block_ab[2 * blk + 1];
   const int c0 = B.block_chunk_begin[blk], c1 = B.block_chunk_begin[blk + 1];
-  R v = R(0);
-  for (int c = c0; c < c1; ++c) v += Ptrs<R>::p(B.ppart)[(size_t)c * 36 + t];
+  const Acc<R>* part = reinterpret_cast<const Acc<R>*>(B.ppart);
+  Acc<R> v;
+  v.zero();
+  for (int c = c0; c < c1; ++c) v.add(part[(size_t)c * 36 + t]);
   const int r = t / 6, q = t % 6;
   if (a == bb) {
-    const R h = Ptrs<R>::p(B.Hpp)[(size_t)a * 36 + t];
-    double d = (double)(h - v);
+    double d = B.Hpp[(size_t)a * 36 + t] - v.value();
     if (r == q) d += B.lm->lambda;
     B.S[(size_t)(6 * a + r) * ld + 6 * a + q] = d;
   } else {
-    const double d = (double)(-v);
+    const double d = -v.value();
     B.S[(size_t)(6 * a + r) * ld + 6 * bb + q] = d;
     B.S[(size_t)(6 * bb + q) * ld + 6 * a + r] = d;
   }
@@ -431,32 +440,37 @@ __global__ void k_schur_assemble(Bufs B, int ld) {
 template <typename R>
 __global__ void k_bschur(Bufs B, int ld) {
   const int a = blockIdx.x;
-  __shared__ R sh[32];
+  __shared__ Acc<R> sh[6][32];
   const int e0 = B.pose_canon_begin[a], e1 = B.pose_canon_begin[a + 1];
-  R s[6];
+  Acc<R> s[6];
 #pragma unroll
-  for (int k = 0; k < 6; ++k) s[k] = R(0);
+  for (int k = 0; k < 6; ++k) s[k].zero();
   for (int i = e0 + threadIdx.x; i < e1; i += blockDim.x) {
     const R* q = Ptrs<R>::p(B.yq) + (size_t)B.pose_canon_list[i] * kYQ + 18;
 #pragma unroll
-    for (int k = 0; k < 6; ++k) s[k] += q[k];
+    for (int k = 0; k < 6; ++k) s[k].add(q[k]);
   }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < 6; ++k) {
-    const R tot = block_sum(s[k], sh);
-    if (threadIdx.x == 0) {
-      const R bp = Ptrs<R>::p(B.b)[6 * (size_t)a + k];
-      B.S[(size_t)ld * ld + 6 * a + k] = (double)(bp - tot);
-    }
-    __syncthreads();
+    const Acc<R> w = warp_sum_acc(s[k]);
+    if (lane == 0) sh[k][wid] = w;
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    Acc<R> tot = sh[threadIdx.x][0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) tot.add(sh[threadIdx.x][w]);
+    B.S[(size_t)ld * ld + 6 * a + threadIdx.x] = B.bp[6 * (size_t)a + threadIdx.x] - tot.value();
   }
 }
 
 // ------------------------------------------------ blocked Cholesky --
 // Diagonal tile k: LL^T in shared memory; a pivot <= 0 marks the solve as
 // failed (SimplicialLLT's info() != Success, linear_solver_eigen.h:118-126).
-__global__ void __launch_bounds__(256) k_chol_potrf(double* S, int ld, int k, LMState* lm) {
+// The reciprocals of the diagonal go to dinv for the triangular solves.
+__global__ void __launch_bounds__(256) k_chol_potrf(double* S, double* dinv, int ld, int k, LMState* lm) {
   __shared__ double T[kNB][kNB + 1];
+  __shared__ double rinv;
   const int o = k * kNB;
   for (int idx = threadIdx.x; idx < kNB * kNB; idx += blockDim.x) {
     const int i = idx / kNB, j = idx % kNB;
@@ -467,10 +481,13 @@ __global__ void __launch_bounds__(256) k_chol_potrf(double* S, int ld, int k, LM
     if (threadIdx.x == 0) {
       const double d = T[kk][kk];
       if (d <= 0.0) lm->solve_ok = 0;
-      T[kk][kk] = sqrt(d);
+      const double r = sqrt(d);
+      T[kk][kk] = r;
+      rinv = 1.0 / r;
+      dinv[o + kk] = rinv;
     }
     __syncthreads();
-    if (threadIdx.x > kk && threadIdx.x < kNB) T[threadIdx.x][kk] /= T[kk][kk];
+    if (threadIdx.x > kk && threadIdx.x < kNB) T[threadIdx.x][kk] *= rinv;
     __syncthreads();
     for (int idx = threadIdx.x; idx < kNB * kNB; idx += blockDim.x) {
       const int i = idx / kNB, j = idx % kNB;
@@ -486,21 +503,23 @@ __global__ void __launch_bounds__(256) k_chol_potrf(double* S, int ld, int k, LM
 
 // Rows below the diagonal tile (8 rows per CTA, the extra b row included):
 // L_ik = A_ik L_kk^-T.
-__global__ void __launch_bounds__(256) k_chol_trsm(double* S, int ld, int k, int nrows) {
+__global__ void __launch_bounds__(256) k_chol_trsm(double* S, const double* dinv, int ld, int k, int nrows) {
   __shared__ double L[kNB][kNB + 1];
   __shared__ double X[8][kNB + 1];
+  __shared__ double di[kNB];
   const int o = k * kNB;
   const int row0 = o + kNB + blockIdx.x * 8;
   for (int idx = threadIdx.x; idx < kNB * kNB; idx += blockDim.x) {
     const int i = idx / kNB, j = idx % kNB;
     L[i][j] = (j <= i) ? S[(size_t)(o + i) * ld + o + j] : 0.0;
   }
+  if (threadIdx.x < kNB) di[threadIdx.x] = dinv[o + threadIdx.x];
   const int r = threadIdx.x / kNB, c = threadIdx.x % kNB;
   const int grow = row0 + r;
   X[r][c] = (grow < nrows) ? S[(size_t)grow * ld + o + c] : 0.0;
   __syncthreads();
   for (int kk = 0; kk < kNB; ++kk) {
-    if (c == kk) X[r][kk] /= L[kk][kk];
+    if (c == kk) X[r][kk] *= di[kk];
     __syncthreads();
     if (c > kk) X[r][c] -= X[r][kk] * L[c][kk];
     __syncthreads();
@@ -531,27 +550,36 @@ __global__ void __launch_bounds__(64) k_chol_syrk(double* S, int ld, int k, int 
   S[(size_t)grow * ld + gcol] -= s;
 }
 
-// L^T x = y with y in the extra row; writes x_p when the factorisation succeeded.
-__global__ void __launch_bounds__(256) k_chol_backsolve(const double* S, int ld, int n, double* x, LMState* lm) {
+// L^T x = y with y in the extra row; writes x_p when the factorisation
+// succeeded.  Each tile column is first staged in shared memory.
+__global__ void __launch_bounds__(256) k_chol_backsolve(const double* S, const double* dinv, int ld, int n,
+                                                        double* x, LMState* lm) {
   if (!lm->solve_ok) return;
   __shared__ double xs[4096 + kNB];
   __shared__ double part[8][kNB];
+  __shared__ double Lt[kNB][kNB + 1];
   const double* y = S + (size_t)ld * ld;
   const int nt = ld / kNB;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int I = nt - 1; I >= 0; --I) {
     const int o = I * kNB;
     double acc = 0.0;
+#pragma unroll 4
     for (int kr = o + kNB + wid; kr < ld; kr += 8) acc += S[(size_t)kr * ld + o + lane] * xs[kr];
     part[wid][lane] = acc;
+    for (int idx = threadIdx.x; idx < kNB * kNB; idx += blockDim.x) {
+      const int i = idx / kNB, j = idx % kNB;
+      Lt[i][j] = (j <= i) ? S[(size_t)(o + i) * ld + o + j] : 0.0;
+    }
     __syncthreads();
     if (wid == 0) {
       double rc = y[o + lane];
 #pragma unroll
       for (int w = 0; w < 8; ++w) rc -= part[w][lane];
+      const double dl = dinv[o + lane];
       for (int c = kNB - 1; c >= 0; --c) {
-        const double xc = __shfl_sync(0xffffffffu, rc / S[(size_t)(o + c) * ld + o + c], c);
-        if (lane < c) rc -= S[(size_t)(o + c) * ld + o + lane] * xc;
+        const double xc = __shfl_sync(0xffffffffu, rc * dl, c);
+        if (lane < c) rc -= Lt[c][lane] * xc;
         if (lane == c) xs[o + c] = xc;
       }
     }
@@ -571,7 +599,7 @@ __global__ void k_backsub(Bufs B, int Lf, int n) {
   double sc = 0.0;
   if (l < Lf) {
     double* xl = B.x + n + 3 * (size_t)l;
-    const R* bl = Ptrs<R>::p(B.b) + n + 3 * (size_t)l;
+    const R* bl = Ptrs<R>::p(B.bl) + 3 * (size_t)l;
     if (B.lm->solve_ok) {
       R cl[3] = {bl[0], bl[1], bl[2]};
       for (int e = B.pt_begin[l]; e < B.pt_begin[l + 1]; ++e) {
@@ -646,7 +674,7 @@ __global__ void k_update_poses(Bufs B, int Kf, int slot0) {
     B.pd[cand][id] = d;
     B.pf[cand][id] = f;
 #pragma unroll
-    for (int k = 0; k < 6; ++k) sc += u[k] * (lam * u[k] + (double)Ptrs<R>::p(B.b)[6 * (size_t)i + k]);
+    for (int k = 0; k < 6; ++k) sc += u[k] * (lam * u[k] + B.bp[6 * (size_t)i + k]);
   }
   const double tot = block_sum(sc, sh);
   if (threadIdx.x == 0) B.scale_part[slot0 + blockIdx.x] = tot;
@@ -692,7 +720,7 @@ __global__ void k_trial_begin(LMState* lm) {
 }
 
 // One LM trial's decision (optimization_algorithm_levenberg.cpp:113-141).
-__global__ void k_lm_decide(Bufs B, int ncost, int nscale) {
+__global__ void k_lm_decide(Bufs B, int ncost, int nscale, cudaGraphConditionalHandle h_trial, int in_graph) {
   __shared__ double sh[32];
   const double tempChi0 = sum_partials(B.cost_part, ncost, sh);
   __syncthreads();
@@ -740,18 +768,52 @@ __global__ void k_lm_decide(Bufs B, int ncost, int nscale) {
   lm->scale = scale;
   lm->last_accepted = accepted ? 1 : 0;
   if (!brk) lm->trial++;
-  const bool more = !brk && rho < 0 && lm->trial < lm->max_trials;
+  const bool more = !brk && rho < 0 && lm->trial < lm->max_trials &&
+                    lm->total_trials < lm->max_iters * lm->max_trials;
   lm->trial_continue = more ? 1 : 0;
   if (!more) {
     if (lm->trial == lm->max_trials || rho == 0 || !isfinite(lm->lambda)) lm->terminate = 1;
     lm->iteration++;
   }
+  if (in_graph) cudaGraphSetConditional(h_trial, more ? 1u : 0u);
 }
 
-__global__ void k_iter_begin(LMState* lm) {
+// LM state at the start of a solve (OptimizationAlgorithmLevenberg members
+// before iteration 0); in a graph it also arms the iteration loop.
+__global__ void k_lm_reset(LMState* lm, int max_trials, int max_log, int max_iters,
+                           cudaGraphConditionalHandle h_iter, int in_graph) {
+  LMState z{};
+  z.cur = 0;
+  z.solve_ok = 1;
+  z.max_trials = max_trials;
+  z.max_log = max_log;
+  z.max_iters = max_iters;
+  z.lambda = -1;
+  z.ni = 2;
+  *lm = z;
+  if (in_graph) cudaGraphSetConditional(h_iter, max_iters > 0 ? 1u : 0u);
+}
+
+// End of one LM iteration (SparseOptimizer::optimize loop condition,
+// sparse_optimizer.cpp:388): continue while not terminated and below the
+// iteration count; the trial total is capped as a safety bound.
+// The loop body has run outer_runs times; that count alone bounds the loop,
+// whatever the trial loop did.
+__global__ void k_iter_end(LMState* lm, cudaGraphConditionalHandle h_iter) {
+  lm->outer_runs++;
+  const bool go = !lm->terminate && lm->iteration < lm->max_iters && lm->outer_runs < lm->max_iters;
+  cudaGraphSetConditional(h_iter, go ? 1u : 0u);
+}
+
+// Start of one LM iteration.  In the captured loop this also re-arms the
+// trial loop: a conditional handle's default value is applied only when the
+// whole graph is launched, so without this the inner WHILE would run zero
+// times from the second iteration on.
+__global__ void k_iter_begin(LMState* lm, cudaGraphConditionalHandle h_trial, int in_graph) {
   if (threadIdx.x == 0) {
     lm->trial = 0;
     lm->trial_continue = 1;
+    if (in_graph) cudaGraphSetConditional(h_trial, 1u);
   }
 }
 
@@ -825,8 +887,8 @@ class Solver {
       block_ab, block_chunk_begin, pose_canon_begin, pose_canon_list, free_pose_ids, free_point_ids;
   DBuf<int2> pairs;
   // numerics
-  DBuf<char> rows, partials, Hpp, Hll, b, yq, ppart;
-  DBuf<double> S, x, cost_part, scale_part, chi2_out;
+  DBuf<char> rows, partials, Hll, bl, yq, ppart;
+  DBuf<double> Hpp, bp, S, dinv, x, cost_part, scale_part, chi2_out;
   DBuf<LMState> lm;
   DBuf<mcba_trial_log> log;
   LMState* lm_host = nullptr;
@@ -836,6 +898,20 @@ class Solver {
   Launch L{};
   bool uploaded = false;
   int64_t launches = 0;
+  int generation = 0;
+  // captured LM loop
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int g_gen = -1, g_iters = -1, g_trials = -1, g_restore = -1;
+  int64_t g_prologue = 0, g_per_iter = 0, g_per_trial = 0;
+
+  void graph_release() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (graph) cudaGraphDestroy(graph);
+    gexec = nullptr;
+    graph = nullptr;
+    g_gen = -1;
+  }
 
   cudaEvent_t next_event() {
     if (evnext == evpool.size()) {
@@ -849,8 +925,9 @@ class Solver {
   ~Solver() {
     cudaSetDevice(device);
     if (stream) cudaStreamSynchronize(stream);
+    graph_release();
     DBuf<double>* ds[] = {&pose_qt[0], &pose_qt[1], &Xd[0], &Xd[1], &pose_qt0, &Xd0,
-                          &S, &x, &cost_part, &scale_part, &chi2_out};
+                          &Hpp, &bp, &S, &dinv, &x, &cost_part, &scale_part, &chi2_out};
     for (auto* d : ds) d->release();
     pd[0].release();
     pd[1].release();
@@ -869,7 +946,7 @@ class Solver {
                        &free_pose_ids, &free_point_ids};
     for (auto* d : is) d->release();
     pairs.release();
-    DBuf<char>* cs[] = {&rows, &partials, &Hpp, &Hll, &b, &yq, &ppart};
+    DBuf<char>* cs[] = {&rows, &partials, &Hll, &bl, &yq, &ppart};
     for (auto* d : cs) d->release();
     lm.release();
     log.release();
@@ -1060,11 +1137,13 @@ Bufs make_bufs(Solver* s) {
   B.rows = s->rows.p;
   B.partials = s->partials.p;
   B.Hpp = s->Hpp.p;
+  B.bp = s->bp.p;
+  B.bl = s->bl.p;
   B.Hll = s->Hll.p;
-  B.b = s->b.p;
   B.yq = s->yq.p;
   B.ppart = s->ppart.p;
   B.S = s->S.p;
+  B.dinv = s->dinv.p;
   B.x = s->x.p;
   B.cost_part = s->cost_part.p;
   B.scale_part = s->scale_part.p;
@@ -1132,7 +1211,8 @@ void launch_linearize(Solver* s, const Bufs& B, const Launch& L, bool first, dou
 }
 
 template <typename R>
-void launch_trial(Solver* s, const Bufs& B, const Launch& L, PhaseClock& pc) {
+void launch_trial(Solver* s, const Bufs& B, const Launch& L, PhaseClock& pc, cudaGraphConditionalHandle h_trial,
+                  int in_graph) {
   cudaStream_t st = s->stream;
   k_trial_begin<<<1, 32, 0, st>>>(B.lm);
   s->launches++;
@@ -1156,11 +1236,11 @@ void launch_trial(Solver* s, const Bufs& B, const Launch& L, PhaseClock& pc) {
     });
     pc.run(MCBA_PHASE_CHOLESKY, [&] {
       for (int k = 0; k < L.tiles; ++k) {
-        k_chol_potrf<<<1, 256, 0, st>>>(B.S, L.ld, k, B.lm);
+        k_chol_potrf<<<1, 256, 0, st>>>(B.S, B.dinv, L.ld, k, B.lm);
         s->launches++;
         const int below = L.nrows - (k + 1) * kNB;
         if (below > 0) {
-          k_chol_trsm<<<(below + 7) / 8, 256, 0, st>>>(B.S, L.ld, k, L.nrows);
+          k_chol_trsm<<<(below + 7) / 8, 256, 0, st>>>(B.S, B.dinv, L.ld, k, L.nrows);
           s->launches++;
           const int rem_cols = L.ld - (k + 1) * kNB;
           if (rem_cols > 0) {
@@ -1170,7 +1250,7 @@ void launch_trial(Solver* s, const Bufs& B, const Launch& L, PhaseClock& pc) {
           }
         }
       }
-      k_chol_backsolve<<<1, 256, 0, st>>>(B.S, L.ld, L.n, B.x, B.lm);
+      k_chol_backsolve<<<1, 256, 0, st>>>(B.S, B.dinv, L.ld, L.n, B.x, B.lm);
       s->launches++;
     });
   }
@@ -1181,7 +1261,7 @@ void launch_trial(Solver* s, const Bufs& B, const Launch& L, PhaseClock& pc) {
   });
   pc.run(MCBA_PHASE_COST, [&] {
     k_cost<R><<<L.ncost, 256, 0, st>>>(B, L.E, 1);
-    k_lm_decide<<<1, 256, 0, st>>>(B, L.ncost, L.nscale_pts + L.nscale_pose);
+    k_lm_decide<<<1, 256, 0, st>>>(B, L.ncost, L.nscale_pts + L.nscale_pose, h_trial, in_graph);
     s->launches += 2;
   });
 }
@@ -1192,13 +1272,16 @@ int alloc_numerics(Solver* s, const Structure& st, std::string* err) {
   const size_t rb = sizeof(R);
   const int nx = L.n + 3 * L.Lf;
   CK(s->rows.ensure(std::max<size_t>(1, (size_t)st.Ec * kRow * rb)));
-  CK(s->partials.ensure(std::max<size_t>(1, (size_t)L.nchunk * 32 * rb)));
-  CK(s->Hpp.ensure(std::max<size_t>(1, (size_t)L.Kf * 36 * rb)));
+  const size_t ab = sizeof(Acc<R>);
+  CK(s->partials.ensure(std::max<size_t>(1, (size_t)L.nchunk * 32 * ab)));
+  CK(s->Hpp.ensure(std::max<size_t>(1, (size_t)L.Kf * 36)));
+  CK(s->bp.ensure(std::max<size_t>(1, (size_t)L.Kf * 6)));
   CK(s->Hll.ensure(std::max<size_t>(1, (size_t)L.Lf * 6 * rb)));
-  CK(s->b.ensure(std::max<size_t>(1, (size_t)nx * rb)));
+  CK(s->bl.ensure(std::max<size_t>(1, (size_t)L.Lf * 3 * rb)));
   CK(s->yq.ensure(std::max<size_t>(1, (size_t)st.Ec * kYQ * rb)));
-  CK(s->ppart.ensure(std::max<size_t>(1, (size_t)L.npc * 36 * rb)));
+  CK(s->ppart.ensure(std::max<size_t>(1, (size_t)L.npc * 36 * ab)));
   CK(s->S.ensure((size_t)(L.ld + kNB) * L.ld));
+  CK(s->dinv.ensure(L.ld));
   CK(s->x.ensure(std::max(nx, 1)));
   CK(s->cost_part.ensure(L.ncost));
   CK(s->scale_part.ensure(L.nscale_pts + L.nscale_pose));
@@ -1206,51 +1289,197 @@ int alloc_numerics(Solver* s, const Structure& st, std::string* err) {
   return MCBA_OK;
 }
 
+// Start of a solve: optional restore of the initial estimates, S padding,
+// x = 0, LM state reset, initial activeRobustChi2.
 template <typename R>
-int run_lm(Solver* s, const RunOptions& o, SolveResult& out, std::string* err) {
+int launch_prologue(Solver* s, const Bufs& B, const RunOptions& o, bool restore, cudaGraphConditionalHandle h_iter,
+                    int in_graph, std::string* err) {
+  const Launch& L = s->L;
+  cudaStream_t st = s->stream;
+  if (restore) {
+    const int r = spread_state(s, true, err);
+    if (r) return r;
+  }
+  const int nx = L.n + 3 * L.Lf;
+  const int max_log = std::max(1, o.iterations * o.max_trials);
+  const size_t total = (size_t)(L.ld + kNB) * L.ld;
+  k_init_S<<<(int)std::min<size_t>((total + 255) / 256, 4096), 256, 0, st>>>(B.S, L.ld, L.n, total);
+  CK(cudaMemsetAsync(B.x, 0, std::max(nx, 1) * sizeof(double), st));
+  k_lm_reset<<<1, 1, 0, st>>>(B.lm, o.max_trials, max_log, o.iterations, h_iter, in_graph);
+  k_cost<R><<<L.ncost, 256, 0, st>>>(B, L.E, 0);
+  k_lm_begin<<<1, 256, 0, st>>>(B, L.ncost);
+  s->launches += 4;
+  CK(cudaGetLastError());
+  return MCBA_OK;
+}
+
+int capture_leaves(cudaStream_t st, std::vector<cudaGraphNode_t>& leaves, std::string* err) {
+  cudaStreamCaptureStatus cs;
+  const cudaGraphNode_t* deps = nullptr;
+  const cudaGraphEdgeData* ed = nullptr;
+  size_t nd = 0;
+  CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, nullptr, &deps, &ed, &nd));
+  leaves.assign(deps, deps + nd);
+  return MCBA_OK;
+}
+
+// The whole LM solve as one CUDA graph: prologue, then
+//   while (iterate) { linearise; while (trial) { Schur, Cholesky, update,
+//   cost, decide }; end-of-iteration test }
+// with both loop conditions set on the device (k_lm_decide, k_iter_end).
+template <typename R>
+int build_graph(Solver* s, const RunOptions& o, bool restore, std::string* err) {
+  s->graph_release();
+  const Launch& L = s->L;
+  const Bufs B = make_bufs(s);
+  cudaStream_t st = s->stream;
+  PhaseClock pc{s, false, {}};
+  cudaGraph_t G;
+  CK(cudaGraphCreate(&G, 0));
+  s->graph = G;
+  cudaGraphConditionalHandle h_iter, h_trial;
+  CK(cudaGraphConditionalHandleCreate(&h_iter, G, 0, cudaGraphCondAssignDefault));
+  std::vector<cudaGraphNode_t> leaves;
+  cudaGraph_t tmp;
+  const int64_t l0 = s->launches;
+  CK(cudaStreamBeginCaptureToGraph(st, G, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  int r = launch_prologue<R>(s, B, o, restore, h_iter, 1, err);
+  if (r) {
+    cudaStreamEndCapture(st, &tmp);
+    return r;
+  }
+  r = capture_leaves(st, leaves, err);
+  CK(cudaStreamEndCapture(st, &tmp));
+  if (r) return r;
+  s->g_prologue = s->launches - l0;
+
+  cudaGraphNodeParams cp{};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h_iter;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t w_iter;
+  CK(cudaGraphAddNode(&w_iter, G, leaves.data(), nullptr, leaves.size(), &cp));
+  cudaGraph_t body_it = cp.conditional.phGraph_out[0];
+  CK(cudaGraphConditionalHandleCreate(&h_trial, body_it, 1, cudaGraphCondAssignDefault));
+
+  const int64_t l1 = s->launches;
+  CK(cudaStreamBeginCaptureToGraph(st, body_it, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  k_iter_begin<<<1, 32, 0, st>>>(B.lm, h_trial, 1);
+  s->launches++;
+  launch_linearize<R>(s, B, L, true, o.tau, pc);
+  r = capture_leaves(st, leaves, err);
+  CK(cudaStreamEndCapture(st, &tmp));
+  if (r) return r;
+
+  cudaGraphNodeParams cp2{};
+  cp2.type = cudaGraphNodeTypeConditional;
+  cp2.conditional.handle = h_trial;
+  cp2.conditional.type = cudaGraphCondTypeWhile;
+  cp2.conditional.size = 1;
+  cudaGraphNode_t w_trial;
+  CK(cudaGraphAddNode(&w_trial, body_it, leaves.data(), nullptr, leaves.size(), &cp2));
+  cudaGraph_t body_tr = cp2.conditional.phGraph_out[0];
+
+  const int64_t l2 = s->launches;
+  CK(cudaStreamBeginCaptureToGraph(st, body_tr, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  launch_trial<R>(s, B, L, pc, h_trial, 1);
+  CK(cudaGetLastError());
+  CK(cudaStreamEndCapture(st, &tmp));
+  s->g_per_trial = s->launches - l2;
+
+  CK(cudaStreamBeginCaptureToGraph(st, body_it, &w_trial, nullptr, 1, cudaStreamCaptureModeRelaxed));
+  k_iter_end<<<1, 1, 0, st>>>(B.lm, h_iter);
+  s->launches++;
+  CK(cudaGetLastError());
+  CK(cudaStreamEndCapture(st, &tmp));
+  s->g_per_iter = (s->launches - l1) - s->g_per_trial;
+  s->launches = l0;
+
+  CK(cudaGraphInstantiate(&s->gexec, G, 0));
+  s->g_gen = s->generation;
+  s->g_iters = o.iterations;
+  s->g_trials = o.max_trials;
+  s->g_restore = restore ? 1 : 0;
+  return MCBA_OK;
+}
+
+template <typename R>
+int finish_run(Solver* s, const RunOptions& o, SolveResult& out, std::string* err) {
+  const Launch& L = s->L;
+  const int max_log = std::max(1, o.iterations * o.max_trials);
+  out.initial_chi2 = s->lm_host->initial_chi;
+  out.final_chi2 = s->lm_host->current_chi;
+  out.lambda = s->lm_host->lambda;
+  out.trials = s->lm_host->total_trials;
+  const int nl = std::min(s->lm_host->n_log, max_log);
+  out.log.resize(nl);
+  if (nl) {
+    CK(cudaMemcpy(out.log.data(), s->log.p, nl * sizeof(mcba_trial_log), cudaMemcpyDeviceToHost));
+    out.d2h += nl * sizeof(mcba_trial_log);
+  }
+  // Hpp of the last linearisation (DumpCalculationGraph)
+  if (L.Kf && out.iterations > 0) {
+    out.hpp.resize((size_t)L.Kf * 36);
+    CK(cudaMemcpy(out.hpp.data(), s->Hpp.p, out.hpp.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    out.d2h += out.hpp.size() * sizeof(double);
+  }
+  return MCBA_OK;
+}
+
+template <typename R>
+int run_lm_graph(Solver* s, const RunOptions& o, bool restore, SolveResult& out, std::string* err) {
+  cudaStream_t stm = s->stream;
+  const int max_log = std::max(1, o.iterations * o.max_trials);
+  CK(s->log.ensure(max_log));
+  if (!s->gexec || s->g_gen != s->generation || s->g_iters != o.iterations || s->g_trials != o.max_trials ||
+      s->g_restore != (restore ? 1 : 0)) {
+    const int r = build_graph<R>(s, o, restore, err);
+    if (r) {
+      s->graph_release();
+      return r;
+    }
+  }
+  CK(cudaEventRecord(s->ev[0], stm));
+  CK(cudaGraphLaunch(s->gexec, stm));
+  CK(cudaEventRecord(s->ev[1], stm));
+  CK(cudaMemcpyAsync(s->lm_host, s->lm.p, sizeof(LMState), cudaMemcpyDeviceToHost, stm));
+  out.d2h += sizeof(LMState);
+  CK(cudaStreamSynchronize(stm));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, s->ev[0], s->ev[1]);
+  out.ms_total = ms;
+  out.iterations = s->lm_host->iteration;
+  const int64_t iters_run = s->lm_host->iteration;
+  s->launches += s->g_prologue + s->g_per_iter * iters_run + s->g_per_trial * s->lm_host->total_trials;
+  return finish_run<R>(s, o, out, err);
+}
+
+template <typename R>
+int run_lm(Solver* s, const RunOptions& o, bool restore, SolveResult& out, std::string* err) {
   const Launch& L = s->L;
   cudaStream_t stm = s->stream;
-  const int nx = L.n + 3 * L.Lf;
   const int iterations = o.iterations, max_trials = o.max_trials;
   const int max_log = std::max(1, iterations * max_trials);
   CK(s->log.ensure(max_log));
-  // S: identity padding, zero b row
-  {
-    const size_t total = (size_t)(L.ld + kNB) * L.ld;
-    k_init_S<<<(int)std::min<size_t>((total + 255) / 256, 4096), 256, 0, stm>>>(s->S.p, L.ld, L.n, total);
-    s->launches++;
-  }
-  CK(cudaMemsetAsync(s->x.p, 0, std::max(nx, 1) * sizeof(double), stm));
-  LMState init{};
-  init.cur = 0;
-  init.solve_ok = 1;
-  init.max_trials = max_trials;
-  init.max_log = max_log;
-  init.lambda = -1;
-  init.ni = 2;
-  *s->lm_host = init;
-  CK(cudaMemcpyAsync(s->lm.p, s->lm_host, sizeof(LMState), cudaMemcpyHostToDevice, stm));
-  out.h2d += sizeof(LMState);
   Bufs B = make_bufs(s);
   PhaseClock pc{s, o.profile, {}};
 
   float ms_lin = 0.f;
   CK(cudaEventRecord(s->ev[0], stm));
-  pc.run(MCBA_PHASE_COST, [&] {
-    k_cost<R><<<L.ncost, 256, 0, stm>>>(B, L.E, 0);
-    k_lm_begin<<<1, 256, 0, stm>>>(B, L.ncost);
-    s->launches += 2;
-  });
+  int r = 0;
+  pc.run(MCBA_PHASE_COST, [&] { r = launch_prologue<R>(s, B, o, restore, 0, 0, err); });
+  if (r) return r;
   int it = 0;
   bool stop = false;
   for (it = 0; it < iterations && !stop; ++it) {
-    k_iter_begin<<<1, 32, 0, stm>>>(B.lm);
+    k_iter_begin<<<1, 32, 0, stm>>>(B.lm, 0, 0);
     s->launches++;
     CK(cudaEventRecord(s->ev[2], stm));
     launch_linearize<R>(s, B, L, it == 0, o.tau, pc);
     CK(cudaEventRecord(s->ev[3], stm));
     for (int t = 0; t < max_trials; ++t) {
-      launch_trial<R>(s, B, L, pc);
+      launch_trial<R>(s, B, L, pc, 0, 0);
       CK(cudaGetLastError());
       CK(cudaMemcpyAsync(s->lm_host, s->lm.p, sizeof(LMState), cudaMemcpyDeviceToHost, stm));
       out.d2h += sizeof(LMState);
@@ -1275,24 +1504,7 @@ int run_lm(Solver* s, const RunOptions& o, SolveResult& out, std::string* err) {
   out.ms_total = ms;
   out.ms_linearize = ms_lin;
   out.iterations = it;
-  out.trials = s->lm_host->total_trials;
-  out.initial_chi2 = s->lm_host->initial_chi;
-  out.final_chi2 = s->lm_host->current_chi;
-  out.lambda = s->lm_host->lambda;
-  const int nl = std::min(s->lm_host->n_log, max_log);
-  out.log.resize(nl);
-  if (nl) {
-    CK(cudaMemcpy(out.log.data(), s->log.p, nl * sizeof(mcba_trial_log), cudaMemcpyDeviceToHost));
-    out.d2h += nl * sizeof(mcba_trial_log);
-  }
-  // Hpp of the last linearisation, FP64 on the host (DumpCalculationGraph)
-  if (L.Kf && iterations > 0) {
-    std::vector<R> h((size_t)L.Kf * 36);
-    CK(cudaMemcpy(h.data(), s->Hpp.p, h.size() * sizeof(R), cudaMemcpyDeviceToHost));
-    out.d2h += h.size() * sizeof(R);
-    out.hpp.assign(h.begin(), h.end());
-  }
-  return MCBA_OK;
+  return finish_run<R>(s, o, out, err);
 }
 
 }  // namespace
@@ -1348,6 +1560,7 @@ int solver_upload(Solver* s, const HostProblem& hp, const Structure& st, SolveRe
   if (r) return r;
   out.h2d += bytes;
   s->uploaded = true;
+  s->generation++;
   return MCBA_OK;
 }
 
@@ -1357,12 +1570,13 @@ int solver_run(Solver* s, const RunOptions& o, bool restore, SolveResult& out, s
     return MCBA_ERR_INVALID;
   }
   CK(cudaSetDevice(s->device));
-  if (restore) {
-    const int r = spread_state(s, true, err);
-    if (r) return r;
-  }
   const int64_t l0 = s->launches;
-  const int r = (s->precision == MCBA_PREC_MIXED) ? run_lm<float>(s, o, out, err) : run_lm<double>(s, o, out, err);
+  const bool graph = o.use_graph && !o.profile;
+  int r;
+  if (s->precision == MCBA_PREC_MIXED)
+    r = graph ? run_lm_graph<float>(s, o, restore, out, err) : run_lm<float>(s, o, restore, out, err);
+  else
+    r = graph ? run_lm_graph<double>(s, o, restore, out, err) : run_lm<double>(s, o, restore, out, err);
   out.launches += s->launches - l0;
   return r;
 }
