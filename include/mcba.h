@@ -280,6 +280,26 @@ int mcba_reproj_backward(int32_t double_precision, int64_t n, const void* pose_q
                          const void* grad_res, void* g_pose, void* g_ext, void* g_X, void* J_pose,
                          void* J_ext, void* J_X, void* stream);
 
+/* ----------------------------------------- allocation-free robust cost -- */
+/* No counterpart in the reference: there every optimiser call allocates.
+ * Sum of rho(e' Omega e) (the quantity of activeRobustChi2) over n mono edges
+ * already in device memory, for callers that must not allocate device memory
+ * -- a tracking thread with a hard per-frame deadline (cudaMalloc/cudaFree can
+ * wait for the whole device) or an application whose own pool owns all device
+ * memory.  Its scratch is a fixed 32 KB file-scope device array shared by all
+ * calls on a device: n is limited to MCBA_NOALLOC_MAX_EDGES (larger n returns
+ * MCBA_ERR_TOO_LARGE) and calls that overlap on the GPU race on the array.
+ * The first call on a device looks the array's device address up; make that
+ * call before any stream capture on the device.
+ * Inputs (device pointers): pose_qt [n][7] T_body_world, ext_qt [n][7]
+ * T_cam_body, X [n][3], K [n][4], obs [n][2], info [n] (NULL: 1), delta [n]
+ * Huber threshold (NULL or <= 0: no kernel), robust [n] (NULL: all robust).
+ * Output: *cost, one device double.  stream is a cudaStream_t or NULL. */
+#define MCBA_NOALLOC_MAX_EDGES (4096 * 256)
+int mcba_robust_cost_noalloc(int64_t n, const double* pose_qt, const double* ext_qt, const double* X,
+                             const double* K, const double* obs, const double* info, const double* delta,
+                             const uint8_t* robust, double* cost, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

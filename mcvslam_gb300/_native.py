@@ -17,6 +17,8 @@ c_u8_p = ctypes.POINTER(ctypes.c_uint8)
 c_i32_p = ctypes.POINTER(ctypes.c_int32)
 
 MCBA_OK = 0
+MCBA_ERR_TOO_LARGE = 9
+NOALLOC_MAX_EDGES = 4096 * 256
 STATUS = {0: "ok", 1: "invalid argument", 2: "nothing to optimise", 3: "not positive definite",
           4: "non-finite input", 5: "timeout", 6: "CUDA error", 7: "out of memory", 8: "no CUDA device",
           9: "too large"}
@@ -115,6 +117,7 @@ def _declare(L):
         "mcba_local_ba": ([P, i32, ctypes.c_float, c_i32_p, c_i32_p], ctypes.c_int),
         "mcba_reproj_forward": ([i32, ctypes.c_int64, P, P, P, P, P, P, P, P, P], ctypes.c_int),
         "mcba_reproj_backward": ([i32, ctypes.c_int64, P, P, P, P, P, P, P, P, P, P, P, P, P, P], ctypes.c_int),
+        "mcba_robust_cost_noalloc": ([ctypes.c_int64, P, P, P, P, P, P, P, P, P, P], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
