@@ -1,0 +1,26 @@
+// mcba_chol.h -- cluster Cholesky solve of the reduced camera system.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+namespace mcba {
+
+struct CholPlan {
+  bool ok = false;
+  int cluster = 0;
+  size_t smem_bytes = 0;
+};
+
+// Chooses a cluster size (16, else 8) whose distributed shared memory holds
+// the n x n system (row stride ld); returns 0 (plan.ok = false) when none does.
+int chol_cluster_plan(int ld, int n, CholPlan* plan);
+
+// Factorises S (row-major, ld columns, identity padding beyond n, b_schur as
+// row ld), solves S x = b and writes x[0..n) -- or sets *solve_ok = 0 and
+// leaves x untouched when a pivot is not positive.
+cudaError_t chol_cluster_launch(const CholPlan& plan, const double* S, int ld, int n, double* x, int* solve_ok,
+                                cudaStream_t st);
+
+}  // namespace mcba

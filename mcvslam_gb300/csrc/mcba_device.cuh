@@ -34,6 +34,19 @@ struct CamF {
   float t[3];
 };
 
+// 1/sqrt(d) for a positive double: FP32 estimate refined by two
+// Newton-Raphson steps y <- y (3 - d y^2) / 2 (quadratic convergence, from
+// ~2^-22 to full precision).  GB300 has little FP64 throughput, so chains of
+// FP64 square roots and divisions are replaced by this and multiplications.
+__device__ __forceinline__ double rsqrt_newton(double d) {
+  if (!(d > 1e-36 && d < 1e36)) return 1.0 / sqrt(d);
+  double y = (double)rsqrtf((float)d);
+  const double hd = 0.5 * d;
+  y = y * (1.5 - hd * y * y);
+  y = y * (1.5 - hd * y * y);
+  return y;
+}
+
 // Unit quaternion (x y z w) -> row-major rotation matrix.
 __device__ __forceinline__ void quat_to_R(const double* q, double* R) {
   const double x = q[0], y = q[1], z = q[2], w = q[3];
@@ -58,9 +71,9 @@ __device__ __forceinline__ void R_to_quat(const double* R, double* q) {
   double x, y, z, w;
   const double tr = R[0] + R[4] + R[8];
   if (tr > 0) {
-    double s = sqrt(tr + 1.0);
-    w = 0.5 * s;
-    s = 0.5 / s;
+    const double a = tr + 1.0, ys = rsqrt_newton(a);
+    w = 0.5 * (a * ys);
+    const double s = 0.5 * ys;
     x = (R[7] - R[5]) * s;
     y = (R[2] - R[6]) * s;
     z = (R[3] - R[1]) * s;
@@ -69,10 +82,10 @@ __device__ __forceinline__ void R_to_quat(const double* R, double* q) {
     if (R[4] > R[0]) i = 1;
     if (R[8] > R[4 * i]) i = 2;
     const int j = (i + 1) % 3, k = (j + 1) % 3;
-    double s = sqrt(R[4 * i] - R[4 * j] - R[4 * k] + 1.0);
+    const double a = R[4 * i] - R[4 * j] - R[4 * k] + 1.0, ys = rsqrt_newton(a);
     double v[3];
-    v[i] = 0.5 * s;
-    s = 0.5 / s;
+    v[i] = 0.5 * (a * ys);
+    const double s = 0.5 * ys;
     w = (R[3 * k + j] - R[3 * j + k]) * s;
     v[j] = (R[3 * j + i] + R[3 * i + j]) * s;
     v[k] = (R[3 * k + i] + R[3 * i + k]) * s;
@@ -86,11 +99,11 @@ __device__ __forceinline__ void R_to_quat(const double* R, double* q) {
     z = -z;
     w = -w;
   }
-  const double n = sqrt(x * x + y * y + z * z + w * w);
-  q[0] = x / n;
-  q[1] = y / n;
-  q[2] = z / n;
-  q[3] = w / n;
+  const double in = rsqrt_newton(x * x + y * y + z * z + w * w);
+  q[0] = x * in;
+  q[1] = y * in;
+  q[2] = z * in;
+  q[3] = w * in;
 }
 
 // Rotate v by the unit quaternion q: v + w*uv + q x uv with uv = 2 q x v.
@@ -110,7 +123,7 @@ __device__ __forceinline__ void quat_rotate(const double* q, const double* v, do
 // normalizeRotation.  qt = x y z w tx ty tz.
 __device__ __forceinline__ void se3_exp_left(const double* u, const double* qt_in, double* qt_out) {
   const double w0 = u[0], w1 = u[1], w2 = u[2];
-  const double theta = sqrt(w0 * w0 + w1 * w1 + w2 * w2);
+  const double th2 = w0 * w0 + w1 * w1 + w2 * w2;
   // Omega = skew(w), Omega^2
   const double O[9] = {0, -w2, w1, w2, 0, -w0, -w1, w0, 0};
   double O2[9];
@@ -119,17 +132,19 @@ __device__ __forceinline__ void se3_exp_left(const double* u, const double* qt_i
 #pragma unroll
     for (int j = 0; j < 3; ++j) O2[3 * i + j] = O[3 * i] * O[j] + O[3 * i + 1] * O[3 + j] + O[3 * i + 2] * O[6 + j];
   double a, b, vb, vc;
-  if (theta < 0.00001) {
+  if (th2 < 1e-10) {  // theta < 1e-5
     a = 1.0;
     b = 0.5;
     vb = 0.5;
     vc = 1.0 / 6.0;
   } else {
-    const double s = sin(theta), c = cos(theta);
-    a = s / theta;
-    b = (1 - c) / (theta * theta);
+    const double inv = rsqrt_newton(th2), theta = th2 * inv;
+    double s, c;
+    sincos(theta, &s, &c);
+    a = s * inv;
+    b = (1 - c) * (inv * inv);
     vb = b;
-    vc = (theta - s) / (theta * theta * theta);
+    vc = (theta - s) * (inv * inv * inv);
   }
   double R[9], V[9];
 #pragma unroll
@@ -156,11 +171,11 @@ __device__ __forceinline__ void se3_exp_left(const double* u, const double* qt_i
     z = -z;
     w = -w;
   }
-  const double n = sqrt(x * x + y * y + z * z + w * w);
-  qt_out[0] = x / n;
-  qt_out[1] = y / n;
-  qt_out[2] = z / n;
-  qt_out[3] = w / n;
+  const double in = rsqrt_newton(x * x + y * y + z * z + w * w);
+  qt_out[0] = x * in;
+  qt_out[1] = y * in;
+  qt_out[2] = z * in;
+  qt_out[3] = w * in;
   qt_out[4] = te[0] + rt[0];
   qt_out[5] = te[1] + rt[1];
   qt_out[6] = te[2] + rt[2];

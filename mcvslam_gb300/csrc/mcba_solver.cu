@@ -34,6 +34,7 @@
 #include <string>
 #include <vector>
 
+#include "mcba_chol.h"
 #include "mcba_device.cuh"
 #include "mcba_internal.h"
 
@@ -46,6 +47,7 @@ constexpr int kRow = 28;   // per canonical edge: Hpl 6x3 | Hll upper 6 | b_l 3 
 constexpr int kYQ = 24;    // per canonical edge: Y 6x3 | q 6
 constexpr int kNB = 32;    // Cholesky tile
 constexpr int kLinThreads = 256;
+constexpr int kClusterCholMaxLd = 512;  // reduced systems up to 85 free keyframes use the cluster solve
 
 // upper-triangle slot of a 6x6 entry (i <= j)
 __host__ __device__ constexpr int u6(int i, int j) { return i * 6 - (i * (i - 1)) / 2 + (j - i); }
@@ -94,6 +96,7 @@ struct Bufs {
   void* bl;         // [3Lf]
   void* yq;         // [Ec][kYQ]
   void* ppart;      // [npchunk][36] accumulators
+  void* qpart;      // [nchunk][6] accumulators of Hpl Dinv b_l per pose chunk
   double* S;        // [(ld+32) x ld]
   double* dinv;     // [ld] reciprocal Cholesky diagonal
   double* x;        // [6Kf + 3Lf]
@@ -117,6 +120,58 @@ __device__ __forceinline__ StateView make_view(const Bufs& B, int which) {
   v.cd = B.cd;
   v.cf = B.cf;
   return v;
+}
+
+// 16-byte vector access to per-edge rows (row strides are multiples of 16 B).
+template <typename R, int N>
+__device__ __forceinline__ void load_row(const R* p, R* v);
+template <typename R, int N>
+__device__ __forceinline__ void store_row(R* p, const R* v);
+template <>
+__device__ __forceinline__ void load_row<float, 20>(const float* p, float* v) {
+  const float4* q = reinterpret_cast<const float4*>(p);
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    const float4 t = q[i];
+    v[4 * i] = t.x;
+    v[4 * i + 1] = t.y;
+    v[4 * i + 2] = t.z;
+    v[4 * i + 3] = t.w;
+  }
+}
+template <>
+__device__ __forceinline__ void load_row<double, 20>(const double* p, double* v) {
+  const double2* q = reinterpret_cast<const double2*>(p);
+#pragma unroll
+  for (int i = 0; i < 10; ++i) {
+    const double2 t = q[i];
+    v[2 * i] = t.x;
+    v[2 * i + 1] = t.y;
+  }
+}
+template <>
+__device__ __forceinline__ void store_row<float, 20>(float* p, const float* v) {
+  float4* q = reinterpret_cast<float4*>(p);
+#pragma unroll
+  for (int i = 0; i < 5; ++i) q[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+}
+template <>
+__device__ __forceinline__ void store_row<double, 20>(double* p, const double* v) {
+  double2* q = reinterpret_cast<double2*>(p);
+#pragma unroll
+  for (int i = 0; i < 10; ++i) q[i] = make_double2(v[2 * i], v[2 * i + 1]);
+}
+template <>
+__device__ __forceinline__ void store_row<float, 28>(float* p, const float* v) {
+  float4* q = reinterpret_cast<float4*>(p);
+#pragma unroll
+  for (int i = 0; i < 7; ++i) q[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+}
+template <>
+__device__ __forceinline__ void store_row<double, 28>(double* p, const double* v) {
+  double2* q = reinterpret_cast<double2*>(p);
+#pragma unroll
+  for (int i = 0; i < 14; ++i) q[i] = make_double2(v[2 * i], v[2 * i + 1]);
 }
 
 // ------------------------------------------------------------ kernels --
@@ -207,8 +262,7 @@ __global__ void __launch_bounds__(kLinThreads) k_linearize(Bufs B) {
         out[24 + i] = bb;
       }
       out[27] = R(0);
-#pragma unroll
-      for (int k = 0; k < kRow; ++k) row[k] = out[k];
+      store_row<R, kRow>(row, out);
     }
     if (r.pose_h >= 0) {
 #pragma unroll
@@ -291,27 +345,39 @@ __global__ void k_point_reduce(Bufs B, int Lf, int n) {
 
 // computeLambdaInit (optimization_algorithm_levenberg.cpp:145-157):
 // tau * max |H_jj| over every free vertex (poses and points).
+// |x| as an order-preserving integer: for non-negative doubles the IEEE bit
+// pattern orders like the value, so the maximum needs no FP64 instruction.
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+}
+
 template <typename R>
 __global__ void k_lambda_init(Bufs B, int Kf, int Lf, double tau) {
-  __shared__ double sh[32];
+  __shared__ unsigned long long sh[32];
   if (B.lm->iteration != 0) return;
-  double m = 0;
-  for (int i = threadIdx.x; i < 6 * Kf; i += blockDim.x)
-    m = fmax(m, fabs(B.Hpp[(size_t)(i / 6) * 36 + 7 * (i % 6)]));
+  unsigned long long m = 0;
+  for (int i = threadIdx.x; i < 6 * Kf; i += blockDim.x) {
+    const unsigned long long v = abs_bits(B.Hpp[(size_t)(i / 6) * 36 + 7 * (i % 6)]);
+    m = v > m ? v : m;
+  }
   for (int i = threadIdx.x; i < 3 * Lf; i += blockDim.x) {
     const int d = i % 3;
-    m = fmax(m, fabs((double)Ptrs<R>::p(B.Hll)[(size_t)(i / 3) * 6 + (d == 0 ? 0 : d == 1 ? 3 : 5)]));
+    const unsigned long long v =
+        abs_bits((double)Ptrs<R>::p(B.Hll)[(size_t)(i / 3) * 6 + (d == 0 ? 0 : d == 1 ? 3 : 5)]);
+    m = v > m ? v : m;
   }
-  m = warp_max(m);
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    const unsigned long long v = __shfl_xor_sync(0xffffffffu, m, o);
+    m = v > m ? v : m;
+  }
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
   __syncthreads();
-  if (threadIdx.x < 32) {
-    double r = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
-    r = warp_max(r);
-    if (threadIdx.x == 0) {
-      B.lm->lambda = tau * r;
-      B.lm->ni = 2.0;
-    }
+  if (threadIdx.x == 0) {
+    unsigned long long r = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = sh[w] > r ? sh[w] : r;
+    B.lm->lambda = tau * __longlong_as_double((long long)r);
+    B.lm->ni = 2.0;
   }
 }
 
@@ -334,30 +400,60 @@ __device__ __forceinline__ void damped_inverse(const R* Hu, R lam, R* Di) {
   Di[8] = (d00 * d11 - d01 * d01) * id;
 }
 
-// Y_e = Hpl_e Dinv, q_e = Hpl_e Dinv b_l for every canonical edge with a free pose.
+// Y_e = Hpl_e Dinv for every edge with a free point and a free pose, walked in
+// the pose-sorted stream (one pose per CTA) so that q = sum_e Hpl_e Dinv b_l
+// -- the coefficient subtracted from b_p (block_solver.hpp:356-374) -- is
+// reduced per chunk without atomics.
 template <typename R>
-__global__ void k_schur_edge(Bufs B, int Ec, int n) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= Ec) return;
-  if (B.canon_pose_h[e] < 0) return;
-  const int l = B.canon_point_h[e];
-  const R lam = (R)B.lm->lambda;
-  R Di[9];
-  damped_inverse<R>(Ptrs<R>::p(B.Hll) + (size_t)l * 6, lam, Di);
-  const R* bl = Ptrs<R>::p(B.bl) + 3 * (size_t)l;
-  R db[3];
+__global__ void __launch_bounds__(kLinThreads) k_schur_edge(Bufs B) {
+  const int c = blockIdx.x;
+  const int jb = B.chunk_begin[c], je = B.chunk_begin[c + 1];
+  const int ph = B.chunk_pose[c];
+  const int j = jb + threadIdx.x;
+  Acc<R> qa[6];
 #pragma unroll
-  for (int i = 0; i < 3; ++i) db[i] = Di[3 * i] * bl[0] + Di[3 * i + 1] * bl[1] + Di[3 * i + 2] * bl[2];
-  const R* H = Ptrs<R>::p(B.rows) + (size_t)e * kRow;
-  R h[18];
+  for (int k = 0; k < 6; ++k) qa[k].zero();
+  if (j < je) {
+    const EdgeRec r = B.recs[j];
+    if (r.canon >= 0 && r.pose_h >= 0) {
+      const int e = r.canon, l = r.point_h;
+      const R lam = (R)B.lm->lambda;
+      R Di[9];
+      damped_inverse<R>(Ptrs<R>::p(B.Hll) + (size_t)l * 6, lam, Di);
+      const R* bl = Ptrs<R>::p(B.bl) + 3 * (size_t)l;
+      R db[3];
 #pragma unroll
-  for (int k = 0; k < 18; ++k) h[k] = H[k];
-  R* o = Ptrs<R>::p(B.yq) + (size_t)e * kYQ;
+      for (int i = 0; i < 3; ++i) db[i] = Di[3 * i] * bl[0] + Di[3 * i + 1] * bl[1] + Di[3 * i + 2] * bl[2];
+      R h[20];
+      load_row<R, 20>(Ptrs<R>::p(B.rows) + (size_t)e * kRow, h);
+      R y[20];
 #pragma unroll
-  for (int r = 0; r < 6; ++r) {
+      for (int rr = 0; rr < 6; ++rr) {
 #pragma unroll
-    for (int c = 0; c < 3; ++c) o[r * 3 + c] = h[r * 3] * Di[c] + h[r * 3 + 1] * Di[3 + c] + h[r * 3 + 2] * Di[6 + c];
-    o[18 + r] = h[r * 3] * db[0] + h[r * 3 + 1] * db[1] + h[r * 3 + 2] * db[2];
+        for (int cc = 0; cc < 3; ++cc)
+          y[rr * 3 + cc] = h[rr * 3] * Di[cc] + h[rr * 3 + 1] * Di[3 + cc] + h[rr * 3 + 2] * Di[6 + cc];
+        qa[rr].add(h[rr * 3] * db[0] + h[rr * 3 + 1] * db[1] + h[rr * 3 + 2] * db[2]);
+      }
+      y[18] = R(0);
+      y[19] = R(0);
+      store_row<R, 20>(Ptrs<R>::p(B.yq) + (size_t)e * kYQ, y);
+    }
+  }
+  if (ph >= 0) {
+    __shared__ Acc<R> sh[6][kLinThreads / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const Acc<R> w = warp_sum_acc(qa[k]);
+      if (lane == 0) sh[k][wid] = w;
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+      Acc<R> t = sh[threadIdx.x][0];
+#pragma unroll
+      for (int w = 1; w < kLinThreads / 32; ++w) t.add(sh[threadIdx.x][w]);
+      reinterpret_cast<Acc<R>*>(B.qpart)[(size_t)c * 6 + threadIdx.x] = t;
+    }
   }
 }
 
@@ -381,12 +477,9 @@ __global__ void __launch_bounds__(256) k_schur_pairs(Bufs B, int npc) {
     const int2 ij = B.pairs[p];
     const R* Y = yq + (size_t)ij.x * kYQ;
     const R* H = rows + (size_t)ij.y * kRow;
-    R y[18], h[18];
-#pragma unroll
-    for (int k = 0; k < 18; ++k) {
-      y[k] = Y[k];
-      h[k] = H[k];
-    }
+    R y[20], h[20];
+    load_row<R, 20>(Y, y);
+    load_row<R, 20>(H, h);
 #pragma unroll
     for (int r = 0; r < 6; ++r)
 #pragma unroll
@@ -428,39 +521,18 @@ __global__ void k_schur_assemble(Bufs B, int ld) {
     double d = B.Hpp[(size_t)a * 36 + t] - v.value();
     if (r == q) d += B.lm->lambda;
     B.S[(size_t)(6 * a + r) * ld + 6 * a + q] = d;
+    if (t < 6) {
+      // b_schur = b_p - sum of the pose's q chunk partials
+      const Acc<R>* qp = reinterpret_cast<const Acc<R>*>(B.qpart);
+      Acc<R> qs;
+      qs.zero();
+      for (int ch = B.pose_chunk_begin[a]; ch < B.pose_chunk_begin[a + 1]; ++ch) qs.add(qp[(size_t)ch * 6 + t]);
+      B.S[(size_t)ld * ld + 6 * a + t] = B.bp[6 * (size_t)a + t] - qs.value();
+    }
   } else {
     const double d = -v.value();
     B.S[(size_t)(6 * a + r) * ld + 6 * bb + q] = d;
     B.S[(size_t)(6 * bb + q) * ld + 6 * a + r] = d;
-  }
-}
-
-// b_schur = b_p - sum_e q_e over the pose's canonical edges, written as the
-// extra row of the factorised matrix.
-template <typename R>
-__global__ void k_bschur(Bufs B, int ld) {
-  const int a = blockIdx.x;
-  __shared__ Acc<R> sh[6][32];
-  const int e0 = B.pose_canon_begin[a], e1 = B.pose_canon_begin[a + 1];
-  Acc<R> s[6];
-#pragma unroll
-  for (int k = 0; k < 6; ++k) s[k].zero();
-  for (int i = e0 + threadIdx.x; i < e1; i += blockDim.x) {
-    const R* q = Ptrs<R>::p(B.yq) + (size_t)B.pose_canon_list[i] * kYQ + 18;
-#pragma unroll
-    for (int k = 0; k < 6; ++k) s[k].add(q[k]);
-  }
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-  for (int k = 0; k < 6; ++k) {
-    const Acc<R> w = warp_sum_acc(s[k]);
-    if (lane == 0) sh[k][wid] = w;
-  }
-  __syncthreads();
-  if (threadIdx.x < 6) {
-    Acc<R> tot = sh[threadIdx.x][0];
-    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) tot.add(sh[threadIdx.x][w]);
-    B.S[(size_t)ld * ld + 6 * a + threadIdx.x] = B.bp[6 * (size_t)a + threadIdx.x] - tot.value();
   }
 }
 
@@ -737,7 +809,8 @@ __global__ void k_lm_decide(Bufs B, int ncost, int nscale, cudaGraphConditionalH
   const bool accepted = (rho > 0) && isfinite(tempChi);
   bool brk = false;
   if (accepted) {
-    double alpha = 1. - pow((2 * rho - 1), 3);
+    const double q = 2 * rho - 1;
+    double alpha = 1. - q * q * q;
     alpha = fmin(alpha, 2. / 3.);
     const double sf = fmax(1. / 3., alpha);
     lm->lambda *= sf;
@@ -887,7 +960,7 @@ class Solver {
       block_ab, block_chunk_begin, pose_canon_begin, pose_canon_list, free_pose_ids, free_point_ids;
   DBuf<int2> pairs;
   // numerics
-  DBuf<char> rows, partials, Hll, bl, yq, ppart;
+  DBuf<char> rows, partials, Hll, bl, yq, ppart, qpart;
   DBuf<double> Hpp, bp, S, dinv, x, cost_part, scale_part, chi2_out;
   DBuf<LMState> lm;
   DBuf<mcba_trial_log> log;
@@ -896,6 +969,7 @@ class Solver {
   std::vector<cudaEvent_t> evpool;
   size_t evnext = 0;
   Launch L{};
+  CholPlan chol;
   bool uploaded = false;
   int64_t launches = 0;
   int generation = 0;
@@ -946,7 +1020,7 @@ class Solver {
                        &free_pose_ids, &free_point_ids};
     for (auto* d : is) d->release();
     pairs.release();
-    DBuf<char>* cs[] = {&rows, &partials, &Hll, &bl, &yq, &ppart};
+    DBuf<char>* cs[] = {&rows, &partials, &Hll, &bl, &yq, &ppart, &qpart};
     for (auto* d : cs) d->release();
     lm.release();
     log.release();
@@ -1142,6 +1216,7 @@ Bufs make_bufs(Solver* s) {
   B.Hll = s->Hll.p;
   B.yq = s->yq.p;
   B.ppart = s->ppart.p;
+  B.qpart = s->qpart.p;
   B.S = s->S.p;
   B.dinv = s->dinv.p;
   B.x = s->x.p;
@@ -1218,10 +1293,8 @@ void launch_trial(Solver* s, const Bufs& B, const Launch& L, PhaseClock& pc, cud
   s->launches++;
   if (L.Kf) {
     pc.run(MCBA_PHASE_SCHUR_EDGE, [&] {
-      if (L.Ec) {
-        k_schur_edge<R><<<(L.Ec + 127) / 128, 128, 0, st>>>(B, L.Ec, L.n);
-        s->launches++;
-      }
+      k_schur_edge<R><<<L.nchunk, kLinThreads, 0, st>>>(B);
+      s->launches++;
     });
     pc.run(MCBA_PHASE_SCHUR_PAIRS, [&] {
       if (L.npc) {
@@ -1231,10 +1304,14 @@ void launch_trial(Solver* s, const Bufs& B, const Launch& L, PhaseClock& pc, cud
     });
     pc.run(MCBA_PHASE_SCHUR_ASSEMBLE, [&] {
       k_schur_assemble<R><<<L.nblk, 64, 0, st>>>(B, L.ld);
-      k_bschur<R><<<L.Kf, 256, 0, st>>>(B, L.ld);
-      s->launches += 2;
+      s->launches++;
     });
     pc.run(MCBA_PHASE_CHOLESKY, [&] {
+      if (s->chol.ok) {
+        chol_cluster_launch(s->chol, B.S, L.ld, L.n, B.x, &B.lm->solve_ok, st);
+        s->launches++;
+        return;
+      }
       for (int k = 0; k < L.tiles; ++k) {
         k_chol_potrf<<<1, 256, 0, st>>>(B.S, B.dinv, L.ld, k, B.lm);
         s->launches++;
@@ -1280,6 +1357,7 @@ int alloc_numerics(Solver* s, const Structure& st, std::string* err) {
   CK(s->bl.ensure(std::max<size_t>(1, (size_t)L.Lf * 3 * rb)));
   CK(s->yq.ensure(std::max<size_t>(1, (size_t)st.Ec * kYQ * rb)));
   CK(s->ppart.ensure(std::max<size_t>(1, (size_t)L.npc * 36 * ab)));
+  CK(s->qpart.ensure(std::max<size_t>(1, (size_t)L.nchunk * 6 * ab)));
   CK(s->S.ensure((size_t)(L.ld + kNB) * L.ld));
   CK(s->dinv.ensure(L.ld));
   CK(s->x.ensure(std::max(nx, 1)));
@@ -1558,6 +1636,8 @@ int solver_upload(Solver* s, const HostProblem& hp, const Structure& st, SolveRe
   }
   r = (s->precision == MCBA_PREC_MIXED) ? alloc_numerics<float>(s, st, err) : alloc_numerics<double>(s, st, err);
   if (r) return r;
+  s->chol = CholPlan();
+  if (L.ld <= kClusterCholMaxLd && L.n > 0) chol_cluster_plan(L.ld, L.n, &s->chol);
   out.h2d += bytes;
   s->uploaded = true;
   s->generation++;
