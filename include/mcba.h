@@ -258,6 +258,30 @@ int mcba_pose_optimization(mcba_problem* p, int32_t rounds, int32_t iterations, 
 int mcba_local_ba(mcba_problem* p, int32_t iterations, float chi2_threshold, int32_t* success_edges,
                   int32_t* written);
 
+/* --------------------------------------------- batched pose-only solve -- */
+/* Many independent PoseEstimation::PoseOptimization problems
+ * (src/PoseEstimation.cpp:48-130) of uneven size in one device pass: a
+ * persistent kernel takes problems from a work queue, one CTA per problem,
+ * and runs `rounds` x `iterations` of g2o's LM on the problem's 6-dof body
+ * pose with the reference's outlier rules (chi2 >= chi2_threshold -> level 1,
+ * robust kernels dropped after round drop_robust_round, early stop below 10
+ * edges).  Problem i owns the unary edges [edge_begin[i], edge_begin[i+1]).
+ *   poses_qt   [n][7]   in: T_body_world (x y z w tx ty tz); out: the result
+ *                       when the reference would call SetPose, else unchanged
+ *   edge_cam [E], edge_obs [E][2], edge_Xw [E][3], edge_info [E], edge_delta [E]
+ *   edge_level [E]      out: 1 for edges classified as outliers
+ *   inliers    [n]      out: nInitial - nBad (0 with fewer than 3 edges)
+ *   ms_device           out: device time of the batch (may be NULL)
+ * cam_K [C][4] and cam_Tcb [C][16] describe the rig shared by all problems.
+ * The launch configuration (threads per CTA, CTAs per SM) is chosen by a
+ * small autotuner on the first call for each batch shape. */
+int mcba_batch_pose_only(int32_t device, int32_t precision, int32_t n, const int32_t* edge_begin,
+                         int32_t n_cams, const float* cam_K, const float* cam_Tcb, const int32_t* edge_cam,
+                         const float* edge_obs, const float* edge_Xw, const float* edge_info,
+                         const float* edge_delta, int32_t rounds, int32_t iterations, float chi2_threshold,
+                         int32_t drop_robust_round, double* poses_qt, uint8_t* edge_level, int32_t* inliers,
+                         double* ms_device);
+
 /* -------------------------------------------- reprojection primitives -- */
 /* Device-pointer entry points behind the autograd harness (no host copies;
  * all pointers are device memory, stream is a cudaStream_t or NULL).  They

@@ -117,6 +117,9 @@ def _declare(L):
         "mcba_local_ba": ([P, i32, ctypes.c_float, c_i32_p, c_i32_p], ctypes.c_int),
         "mcba_reproj_forward": ([i32, ctypes.c_int64, P, P, P, P, P, P, P, P, P], ctypes.c_int),
         "mcba_reproj_backward": ([i32, ctypes.c_int64, P, P, P, P, P, P, P, P, P, P, P, P, P, P], ctypes.c_int),
+        "mcba_batch_pose_only": ([i32, i32, i32, c_i32_p, i32, c_float_p, c_float_p, c_i32_p, c_float_p, c_float_p,
+                                  c_float_p, c_float_p, i32, i32, ctypes.c_float, i32, c_double_p, c_u8_p, c_i32_p,
+                                  c_double_p], ctypes.c_int),
         "mcba_robust_cost_noalloc": ([ctypes.c_int64, P, P, P, P, P, P, P, P, P, P], ctypes.c_int),
     }
     for name, (args, res) in sig.items():

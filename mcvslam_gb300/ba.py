@@ -188,6 +188,49 @@ class Solver:
         N.check(self.L.mcba_dump_hessian(self.h, path.encode()), self.h)
 
 
+def batch_pose_only(problems, precision: str = "mixed", rounds: int = 4, iterations: int = 15,
+                    chi2_thr: float = 5.991, drop_robust_round: int = 2, device: int = 0) -> dict:
+    """PoseOptimization of many single-frame problems in one device pass.
+
+    Each problem is a synth.Problem with one keyframe and fixed points (as
+    produced by synth.pose_only); all problems share the rig of the first.
+    Returns the FP64 poses (x y z w tx ty tz), per-problem inlier counts, the
+    per-edge outlier levels (concatenated in problem order) and the device time."""
+    n = len(problems)
+    counts = np.array([p.n_edges for p in problems], np.int32)
+    edge_begin = np.zeros(n + 1, np.int32)
+    np.cumsum(counts, out=edge_begin[1:])
+    rig = problems[0]
+    # float 4x4 T_body_world -> FP64 quaternion + translation with the library's
+    # own conversion (Converter::toSE3Quat)
+    conv = Solver()
+    for p in problems:
+        T = np.ascontiguousarray(p.pose_Tcw[0], np.float32)
+        N.check(conv.L.mcba_add_keyframe(conv.h, _p(T, N.c_float_p), 0, None), conv.h)
+    conv.n_poses = n
+    qt = np.ascontiguousarray(conv.state()[0])
+    conv.close()
+    cam = np.ascontiguousarray(np.concatenate([p.edge_cam for p in problems]).astype(np.int32))
+    obs = np.ascontiguousarray(np.concatenate([p.edge_obs[:, :2] for p in problems]).astype(np.float32))
+    Xw = np.ascontiguousarray(np.concatenate([p.point_Xw[p.edge_point] for p in problems]).astype(np.float32))
+    info = np.ascontiguousarray(np.concatenate([p.edge_info for p in problems]).astype(np.float32))
+    delta = np.ascontiguousarray(np.concatenate([p.edge_delta for p in problems]).astype(np.float32))
+    level = np.zeros(int(edge_begin[-1]), np.uint8)
+    inliers = np.zeros(n, np.int32)
+    ms = ctypes.c_double(0.0)
+    K = np.ascontiguousarray(rig.cam_K, np.float32)
+    Tcb = np.ascontiguousarray(rig.cam_Tcb, np.float32)
+    L = N.lib()
+    N.check(L.mcba_batch_pose_only(device, PRECISIONS[precision], n, _p(edge_begin, N.c_i32_p), rig.n_cams,
+                                   _p(K, N.c_float_p), _p(Tcb, N.c_float_p), _p(cam, N.c_i32_p),
+                                   _p(obs, N.c_float_p), _p(Xw, N.c_float_p), _p(info, N.c_float_p),
+                                   _p(delta, N.c_float_p), rounds, iterations, chi2_thr, drop_robust_round,
+                                   _p(qt, N.c_double_p), _p(level, N.c_u8_p), _p(inliers, N.c_i32_p),
+                                   ctypes.byref(ms)))
+    return {"pose_qt": qt, "inliers": inliers, "edge_level": level, "edge_begin": edge_begin,
+            "ms_device": ms.value}
+
+
 def solve(pr: synth.Problem, iterations: int = 10, precision: str = "fp64", **kw) -> dict:
     """Load, optimise and read back one problem; returns stats, state and trial log."""
     with Solver(precision=precision, **kw) as s:

@@ -1,0 +1,53 @@
+"""Batched pose-only optimisation (many uneven PoseOptimization problems in
+one persistent launch) against the oracle's PoseOptimization, problem by
+problem: same outlier classification and inlier counts, same pose."""
+import numpy as np
+import pytest
+
+from mcvslam_gb300 import ba, synth
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _problems(sizes, seed0):
+    return [synth.pose_only(int(n), seed=seed0 + i) for i, n in enumerate(sizes)]
+
+
+def _rot(qa, qb):
+    va, vb = qa[:3], qb[:3]
+    w = qa[3] * qb[3] + va @ vb
+    v = qb[3] * va - qa[3] * vb - np.cross(va, vb)
+    return 2 * np.arctan2(np.linalg.norm(v), abs(w))
+
+
+def test_fp64_batch_matches_oracle(gpu):
+    sizes = [2, 8, 40, 300, 700, 1500, 511, 64]
+    probs = _problems(sizes, 4000)
+    out = ba.batch_pose_only(probs, precision="fp64", rounds=4, iterations=10)
+    for i, p in enumerate(probs):
+        o = oracle.pose_optimization(p, rounds=4, iters=10, chi2_thr=5.991)
+        assert out["inliers"][i] == o["ret"], i
+        lv = out["edge_level"][out["edge_begin"][i]:out["edge_begin"][i + 1]]
+        if p.n_edges >= 3:
+            np.testing.assert_array_equal(lv, o["edge_level"])
+        if o["pose_written"]:
+            q = out["pose_qt"][i]
+            assert np.abs(q[4:] - o["pose_qt"][0, 4:]).max() <= 1e-8, i
+            assert _rot(q[:4], o["pose_qt"][0, :4]) <= 1e-8, i
+
+
+def test_mixed_batch_of_uneven_problems(gpu):
+    rng = np.random.default_rng(4100)
+    sizes = rng.integers(500, 6001, 256)
+    probs = _problems(sizes, 5000)
+    mixed = ba.batch_pose_only(probs, precision="mixed", rounds=4, iterations=10)
+    plain = ba.batch_pose_only(probs, precision="fp64", rounds=4, iterations=10)
+    # the FP32 linearisation may move a borderline edge across the chi2 threshold
+    frac_same = np.mean(mixed["edge_level"] == plain["edge_level"])
+    assert frac_same > 0.999
+    assert np.abs(mixed["inliers"] - plain["inliers"]).max() <= max(3, int(0.002 * sizes.max()))
+    for i, p in enumerate(probs):
+        gt = p.gt_pose_Tcw[0]
+        assert np.abs(mixed["pose_qt"][i][4:] - plain["pose_qt"][i][4:]).max() < 1e-4
+    assert mixed["ms_device"] > 0
