@@ -210,22 +210,21 @@ bool compile_structure(const HostProblem& hp, Structure& s) {
     pcnt[(ph >= 0 ? ph : Kf) + 1]++;
   }
   for (int i = 0; i <= Kf; ++i) pcnt[i + 1] += pcnt[i];
+  // inside a pose segment: edges of free points in canonical order (locality
+  // of the scattered per-edge writes), then the others in id order
   std::vector<int32_t> stream(s.E);
   {
     std::vector<int32_t> fill(pcnt.begin(), pcnt.end() - 1);
-    for (int id : act) {
+    for (int e = 0; e < s.Ec; ++e) {
+      const int id = canon_id[e];
       const int ph = ph_of(id);
       stream[fill[ph >= 0 ? ph : Kf]++] = id;
     }
-  }
-  // inside a pose segment, order by canonical position (locality of the
-  // scattered per-edge writes); edges without a free point go last
-  for (int i = 0; i <= Kf; ++i) {
-    std::stable_sort(stream.begin() + pcnt[i], stream.begin() + pcnt[i + 1], [&](int a, int b) {
-      const int ca = canon_of[a] < 0 ? 0x7fffffff : canon_of[a];
-      const int cb = canon_of[b] < 0 ? 0x7fffffff : canon_of[b];
-      return ca < cb;
-    });
+    for (int id : act) {
+      if (canon_of[id] >= 0) continue;
+      const int ph = ph_of(id);
+      stream[fill[ph >= 0 ? ph : Kf]++] = id;
+    }
   }
   s.pose_edge_begin.assign(pcnt.begin(), pcnt.begin() + Kf + 1);
   s.recs.resize(s.E);
@@ -277,7 +276,6 @@ bool compile_structure(const HostProblem& hp, Structure& s) {
   // its free-pose edges (i before j in pose order); two edges of one point on
   // the same pose contribute both orders to the diagonal block.
   std::vector<int32_t> blk_of((size_t)Kf * Kf, -1);
-  std::vector<int64_t> bcount;
   std::vector<int32_t> bab;
   auto visit_pairs = [&](auto&& fn) {
     for (int l = 0; l < Lf; ++l) {
@@ -294,21 +292,22 @@ bool compile_structure(const HostProblem& hp, Structure& s) {
       }
     }
   };
-  // block ids in (a, b) lexicographic order
-  std::vector<uint8_t> present((size_t)Kf * Kf, 0);
-  for (int i = 0; i < Kf; ++i) present[(size_t)i * Kf + i] = 1;
-  visit_pairs([&](int a, int b, int, int) { present[(size_t)a * Kf + b] = 1; });
+  // pairs per reduced-camera block, then block ids in (a, b) lexicographic
+  // order (diagonal blocks always exist)
+  std::vector<int64_t> pcount((size_t)Kf * Kf, 0);
+  visit_pairs([&](int a, int b, int, int) { pcount[(size_t)a * Kf + b]++; });
+  std::vector<int64_t> boff(1, 0);
   for (int a = 0; a < Kf; ++a)
-    for (int b = a; b < Kf; ++b)
-      if (present[(size_t)a * Kf + b]) {
+    for (int b = a; b < Kf; ++b) {
+      const int64_t c = pcount[(size_t)a * Kf + b];
+      if (c || a == b) {
         blk_of[(size_t)a * Kf + b] = (int)bab.size() / 2;
         bab.push_back(a);
         bab.push_back(b);
+        boff.push_back(boff.back() + c);
       }
+    }
   const int nblk = (int)bab.size() / 2;
-  std::vector<int64_t> boff(nblk + 1, 0);
-  visit_pairs([&](int a, int b, int, int) { boff[blk_of[(size_t)a * Kf + b] + 1]++; });
-  for (int k = 0; k < nblk; ++k) boff[k + 1] += boff[k];
   const int64_t npairs = boff[nblk];
   s.pair_ij.resize(2 * (size_t)npairs);
   {
