@@ -421,6 +421,7 @@ class Optimizer {
   std::vector<uint8_t> pose_has_pair;
   // per-vertex edge lists for the threaded accumulation
   std::vector<std::vector<int>> pose_edges, point_edges;
+  std::vector<int> pose_only_edges;  // active edges without a free point
   double lambda = -1, ni = 2;
   orc_result* r = nullptr;
   double t_lin = 0;
@@ -476,12 +477,14 @@ class Optimizer {
     edge_slot.assign(active.size(), -1);
     pose_edges.assign(Kf, {});
     point_edges.assign(Lf, {});
+    pose_only_edges.clear();
     for (size_t a = 0; a < active.size(); ++a) {
       const Edge& e = g.edges[active[a]];
       const int pi = pose_idx[e.pose];
       const int li = (e.type == ORC_EDGE_UNARY) ? -1 : point_idx[e.point];
       if (pi >= 0) pose_edges[pi].push_back((int)a);
       if (li >= 0) point_edges[li].push_back((int)a);
+      if (li < 0) pose_only_edges.push_back((int)a);
       if (pi < 0 || li < 0) continue;
       int found = -1;
       for (int bid : col_blocks[li])
@@ -524,18 +527,30 @@ class Optimizer {
   }
 
   // sparse_optimizer.cpp:102-116 activeRobustChi2
+  double robust_term(const Edge& e) const {
+    if (!e.robust) return edge_chi2(e);
+    double rho[3];
+    huber(edge_chi2(e), e.delta, rho);
+    return rho[0];
+  }
   double robust_chi2() const {
-    double chi = 0.0;
-    for (int id : active) {
-      const Edge& e = g.edges[id];
-      if (e.robust) {
-        double rho[3];
-        huber(edge_chi2(e), e.delta, rho);
-        chi += rho[0];
-      } else {
-        chi += edge_chi2(e);
-      }
+    const int na = (int)active.size();
+    if (n_threads <= 1 || na < 4096) {
+      double chi = 0.0;
+      for (int id : active) chi += robust_term(g.edges[id]);
+      return chi;
     }
+    // static chunks summed in chunk order: deterministic for a thread count
+    std::vector<double> part(n_threads, 0.0);
+#pragma omp parallel for num_threads(n_threads) schedule(static, 1)
+    for (int t = 0; t < n_threads; ++t) {
+      const int a0 = (int)((int64_t)na * t / n_threads), a1 = (int)((int64_t)na * (t + 1) / n_threads);
+      double c = 0.0;
+      for (int a = a0; a < a1; ++a) c += robust_term(g.edges[active[a]]);
+      part[t] = c;
+    }
+    double chi = 0.0;
+    for (double c : part) chi += c;
     return chi;
   }
 
@@ -617,34 +632,53 @@ class Optimizer {
         }
       }
     } else {
-      // threaded variant: per-edge terms in parallel, then a per-vertex
-      // gather in edge order (deterministic; replaces g2o's per-vertex locks)
-      std::vector<EdgeTerms> T(na);
-#pragma omp parallel for num_threads(n_threads) schedule(static)
-      for (int a = 0; a < na; ++a) {
-        Edge& e = g.edges[active[a]];
-        linearize(g, e);
-        const int pi = pose_idx[e.pose];
-        const int li = (e.type == ORC_EDGE_UNARY) ? -1 : point_idx[e.point];
-        edge_terms(e, li >= 0, pi >= 0, T[a]);
-      }
-#pragma omp parallel num_threads(n_threads)
+      // threaded variant: the edges of one free point are linearised and
+      // accumulated by one thread (point terms and Hpl blocks are private to
+      // it); pose terms go to per-thread copies summed in thread order
+      // afterwards (g2o's optional OpenMP build locks the vertices instead)
+#ifdef _OPENMP
+      const int nt = n_threads;
+      priv_pose.assign((size_t)nt * Kf * 42, 0.0);
+#pragma omp parallel num_threads(nt)
       {
+        double* P = &priv_pose[(size_t)omp_get_thread_num() * Kf * 42];
+        EdgeTerms t;
+        auto pose_terms = [&](int pi) {
+          for (int i = 0; i < 6; ++i) P[42 * pi + 36 + i] += t.bp[i];
+          for (int i = 0; i < 36; ++i) P[42 * pi + i] += t.Hpp[i];
+        };
 #pragma omp for schedule(dynamic, 64) nowait
         for (int li = 0; li < Lf; ++li)
           for (int a : point_edges[li]) {
-            for (int i = 0; i < 3; ++i) b[n + 3 * li + i] += T[a].bl[i];
-            for (int i = 0; i < 9; ++i) Hll[9 * li + i] += T[a].Hll[i];
-            if (edge_slot[a] >= 0)
-              for (int i = 0; i < 18; ++i) hpl[edge_slot[a]].B[i] += T[a].Hpl[i];
+            Edge& e = g.edges[active[a]];
+            linearize(g, e);
+            const int pi = pose_idx[e.pose];
+            edge_terms(e, true, pi >= 0, t);
+            for (int i = 0; i < 3; ++i) b[n + 3 * li + i] += t.bl[i];
+            for (int i = 0; i < 9; ++i) Hll[9 * li + i] += t.Hll[i];
+            if (pi >= 0) {
+              for (int i = 0; i < 18; ++i) hpl[edge_slot[a]].B[i] += t.Hpl[i];
+              pose_terms(pi);
+            }
           }
-#pragma omp for schedule(dynamic, 1)
+#pragma omp for schedule(static)
+        for (size_t q = 0; q < pose_only_edges.size(); ++q) {
+          const int a = pose_only_edges[q];
+          Edge& e = g.edges[active[a]];
+          linearize(g, e);
+          const int pi = pose_idx[e.pose];
+          edge_terms(e, false, pi >= 0, t);
+          if (pi >= 0) pose_terms(pi);
+        }
+#pragma omp for schedule(static)
         for (int pi = 0; pi < Kf; ++pi)
-          for (int a : pose_edges[pi]) {
-            for (int i = 0; i < 6; ++i) b[6 * pi + i] += T[a].bp[i];
-            for (int i = 0; i < 36; ++i) Hpp[36 * pi + i] += T[a].Hpp[i];
+          for (int tt = 0; tt < nt; ++tt) {
+            const double* Q = &priv_pose[((size_t)tt * Kf + pi) * 42];
+            for (int i = 0; i < 36; ++i) Hpp[36 * pi + i] += Q[i];
+            for (int i = 0; i < 6; ++i) b[6 * pi + i] += Q[36 + i];
           }
       }
+#endif
     }
     t_lin += tm.s();
     n_lin += na;
@@ -690,7 +724,7 @@ class Optimizer {
         for (int c = r; c < 6; ++c)
           S[(size_t)(6 * i + r) * NP + 6 * i + c] = Hpp[36 * i + 6 * r + c] + (r == c ? lam : 0.0);
     std::fill(coeff.begin(), coeff.end(), 0.0);
-    auto landmark = [&](int li) {
+    auto landmark = [&](int li, double* Sacc, double* cacc, bool locked) {
       double D[9];
       for (int i = 0; i < 9; ++i) D[i] = Hll[9 * li + i];
       D[0] += lam;
@@ -709,26 +743,52 @@ class Optimizer {
         for (int r = 0; r < 6; ++r)
           for (int c = 0; c < 3; ++c)
             BD[r * 3 + c] = Bi.B[r * 3] * Di[c] + Bi.B[r * 3 + 1] * Di[3 + c] + Bi.B[r * 3 + 2] * Di[6 + c];
-        lock_row(i1);
+        if (locked) lock_row(i1);
         for (int r = 0; r < 6; ++r)
-          coeff[6 * i1 + r] += Bi.B[r * 3] * db[0] + Bi.B[r * 3 + 1] * db[1] + Bi.B[r * 3 + 2] * db[2];
+          cacc[6 * i1 + r] += Bi.B[r * 3] * db[0] + Bi.B[r * 3 + 1] * db[1] + Bi.B[r * 3 + 2] * db[2];
         for (size_t q = a; q < col.size(); ++q) {
           const HplBlock& Bj = hpl[col[q]];
           const int i2 = Bj.pose_idx;
           for (int r = 0; r < 6; ++r)
             for (int c = 0; c < 6; ++c) {
               const double v = BD[r * 3] * Bj.B[c * 3] + BD[r * 3 + 1] * Bj.B[c * 3 + 1] + BD[r * 3 + 2] * Bj.B[c * 3 + 2];
-              S[(size_t)(6 * i1 + r) * NP + 6 * i2 + c] -= v;
+              Sacc[(size_t)(6 * i1 + r) * NP + 6 * i2 + c] -= v;
             }
         }
-        unlock_row(i1);
+        if (locked) unlock_row(i1);
       }
     };
     if (n_threads <= 1) {
-      for (int li = 0; li < Lf; ++li) landmark(li);
+      for (int li = 0; li < Lf; ++li) landmark(li, S.data(), coeff.data(), false);
+    } else if ((size_t)NP * NP * n_threads <= ((size_t)8 << 20)) {
+#ifdef _OPENMP
+      // Thread-private reduced-camera accumulators summed afterwards.  g2o's
+      // optional OpenMP build locks block rows instead (block_solver.hpp:
+      // 371-373); with few keyframes that serialises the threads, so the
+      // multi-core baseline accumulates privately when the copies are small.
+      priv_S.assign((size_t)n_threads * NP * NP, 0.0);
+      priv_c.assign((size_t)n_threads * NP, 0.0);
+#pragma omp parallel num_threads(n_threads)
+      {
+        const int t = omp_get_thread_num();
+        double* St = &priv_S[(size_t)t * NP * NP];
+        double* ct = &priv_c[(size_t)t * NP];
+#pragma omp for schedule(dynamic, 16)
+        for (int li = 0; li < Lf; ++li) landmark(li, St, ct, false);
+#pragma omp for schedule(static)
+        for (int row = 0; row < NP; ++row) {
+          double* Sr = &S[(size_t)row * NP];
+          for (int tt = 0; tt < n_threads; ++tt) {
+            const double* Pr = &priv_S[((size_t)tt * NP + row) * NP];
+            for (int c = row - row % 6; c < NP; ++c) Sr[c] += Pr[c];
+            coeff[row] += priv_c[(size_t)tt * NP + row];
+          }
+        }
+      }
+#endif
     } else {
 #pragma omp parallel for num_threads(n_threads) schedule(dynamic, 10)
-      for (int li = 0; li < Lf; ++li) landmark(li);
+      for (int li = 0; li < Lf; ++li) landmark(li, S.data(), coeff.data(), true);
     }
     for (int i = 0; i < NP; ++i) bs[i] = b[i] - coeff[i];
     // LL^T of the upper triangle (diagonal blocks: upper part only)
@@ -747,6 +807,7 @@ class Optimizer {
       x[i] = s / L[(size_t)i * NP + i];
     }
     // landmarks: cl = bl - Hpl^T xp ; xl = Dinv cl
+#pragma omp parallel for num_threads(n_threads) schedule(static) if (n_threads > 1)
     for (int li = 0; li < Lf; ++li) {
       double cl[3] = {b[n + 3 * li], b[n + 3 * li + 1], b[n + 3 * li + 2]};
       for (int bid : col_blocks[li]) {
@@ -792,6 +853,9 @@ class Optimizer {
     for (int k = k0; k < j; ++k) s -= Li[k] * Lj[k];
     L[(size_t)i * NP + j] = s / ljj;
   }
+
+  std::vector<double> priv_S, priv_c;  // thread-private Schur accumulators
+  std::vector<double> priv_pose;  // per-thread pose terms of the threaded linearisation
 
   // Per-row locks for the threaded Schur loop (block_solver.hpp:371-373).
 #ifdef _OPENMP
