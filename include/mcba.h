@@ -59,6 +59,7 @@ typedef struct mcba_options {
   int32_t use_graph;   /* 1: run the LM loop as one CUDA graph with device-side control */
   int32_t profile;     /* 1: time every phase with CUDA events (mcba_stats.ms_phase) */
   void* stream;        /* cudaStream_t to run on, NULL for a library-owned stream */
+  int32_t host_structure; /* 1: compile the problem structure on the host (default 0: on the device) */
 } mcba_options;
 
 /* Phases timed when mcba_options.profile is set, named after g2o's
@@ -112,6 +113,12 @@ typedef struct mcba_trial_log {
 int mcba_abi_version(void);
 const char* mcba_status_string(int status);
 void mcba_default_options(mcba_options* opt);
+/* Handles destroyed with a library-owned stream leave their device workspace
+ * (buffers, pinned staging, stream, captured graph) in a small per-device
+ * cache that the next mcba_create on that device and precision reuses.  This
+ * frees the cached workspaces of one device (device < 0: of every device).
+ * No reference counterpart: g2o allocates per optimizer. */
+int mcba_release_cached(int32_t device);
 int mcba_device_count(int* count);
 
 /* Replaces BAoptimizer::BAoptimizer (src/BAoptimizer.cpp:13-18). */

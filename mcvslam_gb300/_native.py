@@ -27,7 +27,7 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "nothing to optimise", 3: "not posi
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int32), ("device", ctypes.c_int32), ("tau", ctypes.c_double),
                 ("max_trials", ctypes.c_int32), ("use_graph", ctypes.c_int32), ("profile", ctypes.c_int32),
-                ("stream", ctypes.c_void_p)]
+                ("stream", ctypes.c_void_p), ("host_structure", ctypes.c_int32)]
 
 
 class Stats(ctypes.Structure):
@@ -79,6 +79,7 @@ def _declare(L):
         "mcba_status_string": ([ctypes.c_int], ctypes.c_char_p),
         "mcba_default_options": ([ctypes.POINTER(Options)], None),
         "mcba_device_count": ([ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+        "mcba_release_cached": ([i32], ctypes.c_int),
         "mcba_create": ([ctypes.POINTER(Options), ctypes.POINTER(P)], ctypes.c_int),
         "mcba_destroy": ([P], ctypes.c_int),
         "mcba_last_error": ([P], ctypes.c_char_p),

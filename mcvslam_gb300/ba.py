@@ -33,7 +33,7 @@ class Solver:
     """One bundle-adjustment problem on the GPU."""
 
     def __init__(self, precision: str = "fp64", device: int = 0, use_graph: bool = True, tau: float = 1e-5,
-                 max_trials: int = 10, stream: int = 0, profile: bool = False):
+                 max_trials: int = 10, stream: int = 0, profile: bool = False, host_structure: bool = False):
         self.L = N.lib()
         o = N.Options()
         self.L.mcba_default_options(ctypes.byref(o))
@@ -44,6 +44,7 @@ class Solver:
         o.max_trials = max_trials
         o.profile = 1 if profile else 0
         o.stream = stream or None
+        o.host_structure = 1 if host_structure else 0
         h = ctypes.c_void_p()
         N.check(self.L.mcba_create(ctypes.byref(o), ctypes.byref(h)))
         self.h = h

@@ -248,16 +248,17 @@ bool compile_structure(const HostProblem& hp, Structure& s) {
     for (int d = 0; d < 3; ++d) s.obs[3 * (size_t)j + d] = hp.e_obs[3 * (size_t)id + d];
   }
   // chunks: <= kChunk edges, never spanning two poses
+  // the chunks of free pose i are [pose_chunk_begin[i], pose_chunk_begin[i+1]);
+  // the fixed-pose chunks follow from pose_chunk_begin[Kf] on (they hold no
+  // pose terms, so no reduction may read them)
   s.pose_chunk_begin.assign(Kf + 1, 0);
   for (int i = 0; i <= Kf; ++i) {
-    if (i < Kf) s.pose_chunk_begin[i] = (int)s.chunk_pose.size();
+    s.pose_chunk_begin[i] = (int)s.chunk_pose.size();
     for (int a = pcnt[i]; a < pcnt[i + 1]; a += kChunk) {
       s.chunk_begin.push_back(a);
       s.chunk_pose.push_back(i < Kf ? i : -1);
     }
   }
-  s.pose_chunk_begin[Kf] = (int)s.chunk_pose.size();
-  // fixed-pose chunks follow; pose_chunk_begin[Kf] marks where they start
   s.chunk_begin.push_back(s.E);
 
   // canonical edges per free pose (b_schur gather), ascending canonical index
@@ -410,6 +411,11 @@ const char* mcba_status_string(int s) {
   }
 }
 
+int mcba_release_cached(int32_t device) {
+  mcba::solver_release_cached(device);
+  return MCBA_OK;
+}
+
 void mcba_default_options(mcba_options* o) {
   if (!o) return;
   o->precision = MCBA_PREC_FP64;
@@ -419,6 +425,7 @@ void mcba_default_options(mcba_options* o) {
   o->use_graph = 1;
   o->profile = 0;
   o->stream = nullptr;
+  o->host_structure = 0;
 }
 
 int mcba_create(const mcba_options* opt, mcba_problem** out) {
@@ -693,29 +700,54 @@ RunOptions run_options(const mcba_problem* p, int iterations) {
 }
 }  // namespace
 
+namespace {
+// initializeOptimization + buildStructure and the upload of the problem:
+// on the device by default, on the host when mcba_options.host_structure is
+// set.  Returns MCBA_ERR_EMPTY when no vertex is left to optimise.
+int compile_and_upload(mcba_problem* p, SolveResult& res, std::string& e) {
+  StructureSizes z{};
+  int r;
+  if (p->opt.host_structure) {
+    if (!compile_structure(p->hp, p->st)) return MCBA_ERR_EMPTY;
+    r = solver_upload(p->solver, p->hp, &p->st, &z, res, &e);
+  } else {
+    r = solver_upload(p->solver, p->hp, nullptr, &z, res, &e);
+    p->st = Structure();
+    p->st.K = z.K;
+    p->st.P = z.P;
+    p->st.U = z.U;
+    p->st.Kf = z.Kf;
+    p->st.Lf = z.Lf;
+    p->st.E = z.E;
+    p->st.Ec = z.Ec;
+  }
+  return r;
+}
+}  // namespace
+
 int mcba_optimize(mcba_problem* p, int32_t iterations, mcba_stats* st) {
   if (!p || iterations < 0) return fail(p, MCBA_ERR_INVALID, "bad argument");
   if (st) std::memset(st, 0, sizeof(*st));
   int r = ensure_solver(p);
   if (r) return r;
   const auto t0 = std::chrono::steady_clock::now();
-  const bool ok = compile_structure(p->hp, p->st);
+  SolveResult res;
+  std::string e;
+  r = compile_and_upload(p, res, e);
   if (st) {
     st->n_active_edges = p->st.E;
     st->n_free_poses = p->st.Kf;
     st->n_free_points = p->st.Lf;
   }
-  if (!ok) {
+  if (r == MCBA_ERR_EMPTY) {
     p->log.clear();
+    p->prepared = false;
     if (st) {
       st->iterations = -1;
       st->status = MCBA_ERR_EMPTY;
     }
     return fail(p, MCBA_ERR_EMPTY, "0 vertices to optimize");
   }
-  SolveResult res;
-  std::string e;
-  r = solver_upload(p->solver, p->hp, p->st, res, &e);
   const double ms_prep =
       std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   if (!r) r = solver_run(p->solver, run_options(p, iterations), false, res, &e);
@@ -734,10 +766,10 @@ int mcba_prepare(mcba_problem* p) {
   if (!p) return MCBA_ERR_INVALID;
   int r = ensure_solver(p);
   if (r) return r;
-  if (!compile_structure(p->hp, p->st)) return fail(p, MCBA_ERR_EMPTY, "0 vertices to optimize");
   SolveResult res;
   std::string e;
-  r = solver_upload(p->solver, p->hp, p->st, res, &e);
+  r = compile_and_upload(p, res, e);
+  if (r == MCBA_ERR_EMPTY) return fail(p, MCBA_ERR_EMPTY, "0 vertices to optimize");
   if (r) return fail(p, r, e);
   p->prepared = true;
   return MCBA_OK;

@@ -2,6 +2,9 @@
 // the C-ABI layer (mcba_api.cpp) and the device solver (mcba_solver.cu).
 #pragma once
 
+#include <cuda_runtime.h>
+
+#include <algorithm>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -107,10 +110,67 @@ struct Structure {
 // Compiles the active structure; returns false when there is nothing to optimise.
 bool compile_structure(const HostProblem& hp, Structure& s);
 
+// Growable device buffer (reused across calls; never shrinks).
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t n) {
+    if (n <= cap && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    const size_t want = std::max<size_t>(n, 1);
+    cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+// Structure compilation on the device (mcba_compile.cu): the same arrays as
+// compile_structure, built from the raw edge list by scans, a per-point
+// ordering and stable multi-way partitions.
+struct StructureSizes {
+  int K, P, U, Kf, Lf, E, Ec, nchunk, npairs, nblk, npc;
+};
+struct DeviceStructureOut {
+  EdgeRec* recs;
+  float* obs;              // [E][3]
+  int* chunk_begin;        // [nchunk+1]
+  int* chunk_pose;         // [nchunk]
+  int* pose_chunk_begin;   // [Kf+1]
+  int* pt_begin;           // [Lf+1]
+  int* canon_pose_h;       // [Ec]
+  int* canon_point_h;      // [Ec]
+  int2* pairs;             // [npairs]
+  int* pchunk_begin;       // [npc+1]
+  int* block_ab;           // [nblk][2]
+  int* block_chunk_begin;  // [nblk+1]
+  int* pose_canon_begin;   // [Kf+1]
+  int* pose_canon_list;    // [pose_canon_begin[Kf]]
+  int* free_pose_ids;      // [Kf]
+  int* free_point_ids;     // [Lf]
+};
+class DeviceCompiler;
+DeviceCompiler* compiler_create();
+void compiler_destroy(DeviceCompiler* c);
+// Uploads the raw graph and computes every size (one device-to-host read).
+int compiler_phase1(DeviceCompiler* c, const HostProblem& hp, cudaStream_t st, StructureSizes* sz, int64_t* h2d,
+                    std::string* err);
+// Fills the caller's buffers (sized from phase 1).
+int compiler_phase2(DeviceCompiler* c, const DeviceStructureOut& out, cudaStream_t st, std::string* err);
+
 // Device solver (mcba_solver.cu).
 class Solver;
 Solver* solver_create(int device, int precision, void* stream, std::string* err);
 void solver_destroy(Solver* s);
+// Frees the idle solvers kept for reuse (device < 0: all devices); returns how many.
+int solver_release_cached(int device);
 
 struct SolveResult {
   int status = MCBA_OK;
@@ -134,7 +194,11 @@ struct RunOptions {
 };
 
 // Uploads state and structure (keeps a device copy of the initial state).
-int solver_upload(Solver* s, const HostProblem& hp, const Structure& st, SolveResult& out, std::string* err);
+// With st == nullptr the structure is compiled on the device; the sizes of
+// the compiled structure are returned in *sizes either way.  Returns
+// MCBA_ERR_EMPTY when nothing is left to optimise.
+int solver_upload(Solver* s, const HostProblem& hp, const Structure* st, StructureSizes* sizes, SolveResult& out,
+                  std::string* err);
 // Runs LM on the uploaded problem; restore = start again from the uploaded
 // initial state.
 int solver_run(Solver* s, const RunOptions& o, bool restore, SolveResult& out, std::string* err);

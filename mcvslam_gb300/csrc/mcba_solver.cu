@@ -31,6 +31,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -912,27 +913,6 @@ __global__ void k_edge_chi2(const EdgeRec* recs, const float* obs, int E, StateV
 }  // namespace
 
 // ----------------------------------------------------------- host side --
-template <typename T>
-struct DBuf {
-  T* p = nullptr;
-  size_t cap = 0;
-  cudaError_t ensure(size_t n) {
-    if (n <= cap && p) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-    const size_t want = std::max<size_t>(n, 1);
-    cudaError_t e = cudaMalloc(&p, want * sizeof(T));
-    if (e == cudaSuccess) cap = want;
-    return e;
-  }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-  }
-};
-
 namespace {
 struct Launch {
   int nchunk, Kf, Lf, Ec, E, n, npc, nblk, ld, nrows, ncost, nscale_pts, nscale_pose, tiles;
@@ -965,11 +945,13 @@ class Solver {
   DBuf<LMState> lm;
   DBuf<mcba_trial_log> log;
   LMState* lm_host = nullptr;
+  DeviceCompiler* compiler = nullptr;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   std::vector<cudaEvent_t> evpool;
   size_t evnext = 0;
   Launch L{};
   CholPlan chol;
+  int chol_ld = -1, chol_n = -1;
   bool uploaded = false;
   int64_t launches = 0;
   int generation = 0;
@@ -977,6 +959,9 @@ class Solver {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
   int g_gen = -1, g_iters = -1, g_trials = -1, g_restore = -1;
+  double g_tau = 0.0;
+  // what a captured graph bakes in: launch sizes, buffer addresses, solve plan
+  std::vector<char> g_sig;
   int64_t g_prologue = 0, g_per_iter = 0, g_per_trial = 0;
 
   void graph_release() {
@@ -1028,6 +1013,7 @@ class Solver {
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
     for (auto& e : evpool) cudaEventDestroy(e);
+    if (compiler) compiler_destroy(compiler);
     if (own_stream && stream) cudaStreamDestroy(stream);
   }
 };
@@ -1040,6 +1026,15 @@ class Solver {
       return MCBA_ERR_CUDA;                                                        \
     }                                                                              \
   } while (0)
+
+namespace {
+// Idle solvers (library-owned stream) kept for the next handle on the same
+// device and precision: device buffers, pinned staging, events, the stream
+// and the captured graph are reused instead of being allocated again.
+std::mutex g_pool_mu;
+std::vector<Solver*> g_pool;
+constexpr int kPoolPerKey = 2;
+}  // namespace
 
 Solver* solver_create(int device, int precision, void* stream, std::string* err) {
   int n = 0;
@@ -1054,6 +1049,15 @@ Solver* solver_create(int device, int precision, void* stream, std::string* err)
   if (cudaSetDevice(device) != cudaSuccess) {
     if (err) *err = "cudaSetDevice failed";
     return nullptr;
+  }
+  if (!stream) {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    for (size_t i = 0; i < g_pool.size(); ++i)
+      if (g_pool[i]->device == device && g_pool[i]->precision == precision) {
+        Solver* s = g_pool[i];
+        g_pool.erase(g_pool.begin() + (long)i);
+        return s;
+      }
   }
   Solver* s = new Solver();
   s->device = device;
@@ -1077,7 +1081,41 @@ Solver* solver_create(int device, int precision, void* stream, std::string* err)
   return s;
 }
 
-void solver_destroy(Solver* s) { delete s; }
+void solver_destroy(Solver* s) {
+  if (!s) return;
+  if (s->own_stream) {
+    cudaSetDevice(s->device);
+    if (cudaStreamSynchronize(s->stream) == cudaSuccess) {
+      s->uploaded = false;
+      std::lock_guard<std::mutex> lk(g_pool_mu);
+      int same = 0;
+      for (Solver* q : g_pool) same += (q->device == s->device && q->precision == s->precision);
+      if (same < kPoolPerKey) {
+        g_pool.push_back(s);
+        return;
+      }
+    }
+  }
+  delete s;
+}
+
+int solver_release_cached(int device) {
+  std::vector<Solver*> drop;
+  {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    for (size_t i = 0; i < g_pool.size();) {
+      if (device < 0 || g_pool[i]->device == device) {
+        drop.push_back(g_pool[i]);
+        g_pool.erase(g_pool.begin() + (long)i);
+      } else {
+        ++i;
+      }
+    }
+  }
+  for (Solver* s : drop) delete s;
+  return (int)drop.size();
+}
+
 bool solver_has_upload(const Solver* s) { return s && s->uploaded; }
 
 namespace {
@@ -1344,18 +1382,18 @@ void launch_trial(Solver* s, const Bufs& B, const Launch& L, PhaseClock& pc, cud
 }
 
 template <typename R>
-int alloc_numerics(Solver* s, const Structure& st, std::string* err) {
+int alloc_numerics(Solver* s, std::string* err) {
   const Launch& L = s->L;
   const size_t rb = sizeof(R);
   const int nx = L.n + 3 * L.Lf;
-  CK(s->rows.ensure(std::max<size_t>(1, (size_t)st.Ec * kRow * rb)));
+  CK(s->rows.ensure(std::max<size_t>(1, (size_t)L.Ec * kRow * rb)));
   const size_t ab = sizeof(Acc<R>);
   CK(s->partials.ensure(std::max<size_t>(1, (size_t)L.nchunk * 32 * ab)));
   CK(s->Hpp.ensure(std::max<size_t>(1, (size_t)L.Kf * 36)));
   CK(s->bp.ensure(std::max<size_t>(1, (size_t)L.Kf * 6)));
   CK(s->Hll.ensure(std::max<size_t>(1, (size_t)L.Lf * 6 * rb)));
   CK(s->bl.ensure(std::max<size_t>(1, (size_t)L.Lf * 3 * rb)));
-  CK(s->yq.ensure(std::max<size_t>(1, (size_t)st.Ec * kYQ * rb)));
+  CK(s->yq.ensure(std::max<size_t>(1, (size_t)L.Ec * kYQ * rb)));
   CK(s->ppart.ensure(std::max<size_t>(1, (size_t)L.npc * 36 * ab)));
   CK(s->qpart.ensure(std::max<size_t>(1, (size_t)L.nchunk * 6 * ab)));
   CK(s->S.ensure((size_t)(L.ld + kNB) * L.ld));
@@ -1479,6 +1517,7 @@ int build_graph(Solver* s, const RunOptions& o, bool restore, std::string* err) 
   s->g_iters = o.iterations;
   s->g_trials = o.max_trials;
   s->g_restore = restore ? 1 : 0;
+  s->g_tau = o.tau;
   return MCBA_OK;
 }
 
@@ -1511,7 +1550,7 @@ int run_lm_graph(Solver* s, const RunOptions& o, bool restore, SolveResult& out,
   const int max_log = std::max(1, o.iterations * o.max_trials);
   CK(s->log.ensure(max_log));
   if (!s->gexec || s->g_gen != s->generation || s->g_iters != o.iterations || s->g_trials != o.max_trials ||
-      s->g_restore != (restore ? 1 : 0)) {
+      s->g_restore != (restore ? 1 : 0) || s->g_tau != o.tau) {
     const int r = build_graph<R>(s, o, restore, err);
     if (r) {
       s->graph_release();
@@ -1587,60 +1626,139 @@ int run_lm(Solver* s, const RunOptions& o, bool restore, SolveResult& out, std::
 
 }  // namespace
 
-int solver_upload(Solver* s, const HostProblem& hp, const Structure& st, SolveResult& out, std::string* err) {
+int solver_upload(Solver* s, const HostProblem& hp, const Structure* hst, StructureSizes* sizes, SolveResult& out,
+                  std::string* err) {
   CK(cudaSetDevice(s->device));
   s->uploaded = false;
   int64_t bytes = 0;
-  int r = upload_state(s, hp, st.U, bytes, err);
-  if (r) return r;
   cudaStream_t stm = s->stream;
-  CK(up(s->recs, st.recs, stm, bytes));
-  CK(up(s->obs, st.obs, stm, bytes));
-  CK(up(s->chunk_begin, st.chunk_begin, stm, bytes));
-  CK(up(s->chunk_pose, st.chunk_pose, stm, bytes));
-  CK(up(s->pose_chunk_begin, st.pose_chunk_begin, stm, bytes));
-  CK(up(s->pt_begin, st.pt_begin, stm, bytes));
-  CK(up(s->canon_pose_h, st.canon_pose_h, stm, bytes));
-  CK(up(s->canon_point_h, st.canon_point_h, stm, bytes));
-  CK(s->pairs.ensure(std::max<size_t>(1, st.pair_ij.size() / 2)));
-  if (!st.pair_ij.empty()) {
-    CK(cudaMemcpyAsync(s->pairs.p, st.pair_ij.data(), st.pair_ij.size() * sizeof(int32_t), cudaMemcpyHostToDevice, stm));
-    bytes += st.pair_ij.size() * sizeof(int32_t);
+  StructureSizes z{};
+  int r;
+  if (hst) {
+    const Structure& st = *hst;
+    z.K = st.K;
+    z.P = st.P;
+    z.U = st.U;
+    z.Kf = st.Kf;
+    z.Lf = st.Lf;
+    z.E = st.E;
+    z.Ec = st.Ec;
+    z.nchunk = (int)st.chunk_pose.size();
+    z.npairs = (int)(st.pair_ij.size() / 2);
+    z.nblk = (int)(st.block_ab.size() / 2);
+    z.npc = (int)st.pchunk_block.size();
+    if (sizes) *sizes = z;
+    r = upload_state(s, hp, st.U, bytes, err);
+    if (r) return r;
+    CK(up(s->recs, st.recs, stm, bytes));
+    CK(up(s->obs, st.obs, stm, bytes));
+    CK(up(s->chunk_begin, st.chunk_begin, stm, bytes));
+    CK(up(s->chunk_pose, st.chunk_pose, stm, bytes));
+    CK(up(s->pose_chunk_begin, st.pose_chunk_begin, stm, bytes));
+    CK(up(s->pt_begin, st.pt_begin, stm, bytes));
+    CK(up(s->canon_pose_h, st.canon_pose_h, stm, bytes));
+    CK(up(s->canon_point_h, st.canon_point_h, stm, bytes));
+    CK(s->pairs.ensure(std::max<size_t>(1, st.pair_ij.size() / 2)));
+    if (!st.pair_ij.empty()) {
+      CK(cudaMemcpyAsync(s->pairs.p, st.pair_ij.data(), st.pair_ij.size() * sizeof(int32_t), cudaMemcpyHostToDevice, stm));
+      bytes += st.pair_ij.size() * sizeof(int32_t);
+    }
+    CK(up(s->pchunk_begin, st.pchunk_begin, stm, bytes));
+    CK(up(s->block_ab, st.block_ab, stm, bytes));
+    CK(up(s->block_chunk_begin, st.block_chunk_begin, stm, bytes));
+    CK(up(s->pose_canon_begin, st.pose_canon_begin, stm, bytes));
+    CK(up(s->pose_canon_list, st.pose_canon_list, stm, bytes));
+    CK(up(s->free_pose_ids, st.free_pose_ids, stm, bytes));
+    CK(up(s->free_point_ids, st.free_point_ids, stm, bytes));
+  } else {
+    if (!s->compiler) s->compiler = compiler_create();
+    r = compiler_phase1(s->compiler, hp, stm, &z, &bytes, err);
+    if (r) return r;
+    if (sizes) *sizes = z;
+    if (z.Kf + z.Lf == 0 || z.E == 0) return MCBA_ERR_EMPTY;
+    r = upload_state(s, hp, z.U, bytes, err);
+    if (r) return r;
+    CK(s->recs.ensure(z.E));
+    CK(s->obs.ensure(3 * (size_t)z.E));
+    CK(s->chunk_begin.ensure(z.nchunk + 1));
+    CK(s->chunk_pose.ensure(z.nchunk + 1));
+    CK(s->pose_chunk_begin.ensure(z.Kf + 1));
+    CK(s->pt_begin.ensure(z.Lf + 1));
+    CK(s->canon_pose_h.ensure(z.Ec + 1));
+    CK(s->canon_point_h.ensure(z.Ec + 1));
+    CK(s->pairs.ensure(std::max(z.npairs, 1)));
+    CK(s->pchunk_begin.ensure(z.npc + 1));
+    CK(s->block_ab.ensure(2 * (size_t)z.nblk + 2));
+    CK(s->block_chunk_begin.ensure(z.nblk + 1));
+    CK(s->pose_canon_begin.ensure(z.Kf + 1));
+    CK(s->pose_canon_list.ensure(z.Ec + 1));
+    CK(s->free_pose_ids.ensure(z.Kf + 1));
+    CK(s->free_point_ids.ensure(z.Lf + 1));
+    DeviceStructureOut o;
+    o.recs = s->recs.p;
+    o.obs = s->obs.p;
+    o.chunk_begin = s->chunk_begin.p;
+    o.chunk_pose = s->chunk_pose.p;
+    o.pose_chunk_begin = s->pose_chunk_begin.p;
+    o.pt_begin = s->pt_begin.p;
+    o.canon_pose_h = s->canon_pose_h.p;
+    o.canon_point_h = s->canon_point_h.p;
+    o.pairs = s->pairs.p;
+    o.pchunk_begin = s->pchunk_begin.p;
+    o.block_ab = s->block_ab.p;
+    o.block_chunk_begin = s->block_chunk_begin.p;
+    o.pose_canon_begin = s->pose_canon_begin.p;
+    o.pose_canon_list = s->pose_canon_list.p;
+    o.free_pose_ids = s->free_pose_ids.p;
+    o.free_point_ids = s->free_point_ids.p;
+    r = compiler_phase2(s->compiler, o, stm, err);
+    if (r) return r;
   }
-  CK(up(s->pchunk_begin, st.pchunk_begin, stm, bytes));
-  CK(up(s->block_ab, st.block_ab, stm, bytes));
-  CK(up(s->block_chunk_begin, st.block_chunk_begin, stm, bytes));
-  CK(up(s->pose_canon_begin, st.pose_canon_begin, stm, bytes));
-  CK(up(s->pose_canon_list, st.pose_canon_list, stm, bytes));
-  CK(up(s->free_pose_ids, st.free_pose_ids, stm, bytes));
-  CK(up(s->free_point_ids, st.free_point_ids, stm, bytes));
   Launch& L = s->L;
-  const int Kf = st.Kf, Lf = st.Lf, n = 6 * Kf;
-  L.nchunk = (int)st.chunk_pose.size();
+  const int Kf = z.Kf, Lf = z.Lf, n = 6 * Kf;
+  L.nchunk = z.nchunk;
   L.Kf = Kf;
   L.Lf = Lf;
-  L.Ec = st.Ec;
-  L.E = st.E;
+  L.Ec = z.Ec;
+  L.E = z.E;
   L.n = n;
-  L.npc = (int)st.pchunk_block.size();
-  L.nblk = (int)st.block_ab.size() / 2;
+  L.npc = z.npc;
+  L.nblk = z.nblk;
   L.ld = std::max(kNB, ((n + kNB - 1) / kNB) * kNB);
   L.tiles = L.ld / kNB;
   L.nrows = L.ld + 1;  // the b_schur row
-  L.ncost = (st.E + 255) / 256;
+  L.ncost = (z.E + 255) / 256;
   L.nscale_pts = std::max(1, (Lf + 127) / 128);
   L.nscale_pose = std::max(1, (Kf + 127) / 128);
   if (L.ld > 4096) {
     if (err) *err = "reduced camera system above 4096 (682 free keyframes)";
     return MCBA_ERR_TOO_LARGE;
   }
-  r = (s->precision == MCBA_PREC_MIXED) ? alloc_numerics<float>(s, st, err) : alloc_numerics<double>(s, st, err);
+  r = (s->precision == MCBA_PREC_MIXED) ? alloc_numerics<float>(s, err) : alloc_numerics<double>(s, err);
   if (r) return r;
-  s->chol = CholPlan();
-  if (L.ld <= kClusterCholMaxLd && L.n > 0) chol_cluster_plan(L.ld, L.n, &s->chol);
+  if (L.ld != s->chol_ld || L.n != s->chol_n) {
+    s->chol = CholPlan();
+    if (L.ld <= kClusterCholMaxLd && L.n > 0) chol_cluster_plan(L.ld, L.n, &s->chol);
+    s->chol_ld = L.ld;
+    s->chol_n = L.n;
+  }
   out.h2d += bytes;
   s->uploaded = true;
-  s->generation++;
+  // a captured LM graph stays valid while the launch sizes, the buffer
+  // addresses and the solve plan are unchanged (everything else is read from
+  // device memory when it runs)
+  {
+    const Bufs B = make_bufs(s);
+    std::vector<char> sig(sizeof(Launch) + sizeof(Bufs) + 3 * sizeof(size_t));
+    std::memcpy(sig.data(), &L, sizeof(Launch));
+    std::memcpy(sig.data() + sizeof(Launch), &B, sizeof(Bufs));
+    const size_t plan[3] = {(size_t)s->chol.ok, (size_t)s->chol.cluster, s->chol.smem_bytes};
+    std::memcpy(sig.data() + sizeof(Launch) + sizeof(Bufs), plan, sizeof(plan));
+    if (sig != s->g_sig) {
+      s->g_sig.swap(sig);
+      s->generation++;
+    }
+  }
   return MCBA_OK;
 }
 

@@ -190,3 +190,69 @@ def test_profiled_run_reports_every_phase(gpu):
         st = s.optimize(5)
     assert all(n > 0 for n in st["n_phase"])
     assert st["kernel_launches"] > 0 and st["ms_phase"][0] > 0
+
+
+def _solve_both(pr, iters, precision):
+    out = []
+    for host in (True, False):
+        with ba.Solver(precision=precision, device=0, host_structure=host) as s:
+            s.load(pr)
+            st = s.optimize(iters)
+            qt, X = s.state()
+            out.append((st, s.trial_log(), qt, X))
+    return out
+
+
+def _problems():
+    c1 = synth.config(1)
+    lv = c1.copy()
+    lv.edge_level[::7] = 1                      # inactive edges
+    fx = c1.copy()
+    fx.point_fixed[::5] = 1                     # fixed points: edges without a free point
+    fx.pose_fixed[:3] = 1                       # and edges with every vertex fixed
+    un = synth.pose_only(800, seed=5)
+    un.edge_type[:] = synth.EDGE_UNARY         # unary edges with constant points
+    mx = c1.copy()
+    mx.edge_type[::9] = synth.EDGE_UNARY       # unary and binary edges together
+    return [("config1", c1), ("levels", lv), ("fixed", fx), ("stereo", synth.reference_style(3)),
+            ("pose_only", synth.pose_only(800, seed=5)), ("unary", un), ("mixed_types", mx)]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_device_structure_equals_host_structure(precision, gpu):
+    """The structure compiled on the device gives bit-identical solves."""
+    for name, pr in _problems():
+        (sh, lh, qh, xh), (sd, ld, qd, xd) = _solve_both(pr, 6, precision)
+        for k in ("n_active_edges", "n_free_poses", "n_free_points", "iterations", "trials"):
+            assert sh[k] == sd[k], (name, k, sh[k], sd[k])
+        assert sh["final_chi2"] == sd["final_chi2"], name
+        np.testing.assert_array_equal(lh, ld, err_msg=name)
+        np.testing.assert_array_equal(qh, qd, err_msg=name)
+        np.testing.assert_array_equal(xh, xd, err_msg=name)
+
+
+def test_cached_workspaces_give_identical_solves(gpu):
+    """Handles reuse the workspace of destroyed ones (buffers, staging, graph):
+    a solve after a differently sized one equals a solve on a fresh workspace."""
+    from mcvslam_gb300 import _native
+
+    a, b = synth.config(1), synth.reference_style(2)
+
+    def run(pr):
+        with ba.Solver(precision="mixed", device=0) as s:
+            s.load(pr)
+            st = s.optimize(5)
+            return st["final_chi2"], s.trial_log(), s.state()
+
+    _native.lib().mcba_release_cached(-1)
+    first = run(a)
+    run(b)
+    run(a)
+    again = run(a)
+    _native.lib().mcba_release_cached(0)
+    fresh = run(a)
+    for other in (again, fresh):
+        assert other[0] == first[0]
+        np.testing.assert_array_equal(other[1], first[1])
+        np.testing.assert_array_equal(other[2][0], first[2][0])
+        np.testing.assert_array_equal(other[2][1], first[2][1])
