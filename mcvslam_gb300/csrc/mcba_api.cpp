@@ -385,7 +385,8 @@ int push_edge(mcba_problem* p, uint8_t type, int32_t kf, int32_t mp, int32_t cam
   h.e_delta.push_back(delta);
   h.e_robust.push_back(robust);
   h.e_level.push_back(level);
-  for (int d = 0; d < 3; ++d) h.e_Xw.push_back(type == MCBA_EDGE_UNARY ? (double)Xw[d] : 0.0);
+  if (type == MCBA_EDGE_UNARY)
+    for (int d = 0; d < 3; ++d) h.u_Xw.push_back((double)Xw[d]);
   return MCBA_OK;
 }
 
@@ -554,7 +555,7 @@ int mcba_add_edges(mcba_problem* p, int32_t n, const uint8_t* type, const int32_
                    const int32_t* cam, const float* obs, const float* Xw, const float* info, const float* delta,
                    int32_t* first_id) {
   if (!p || n < 0 || (n > 0 && (!type || !kf || !cam || !obs))) return fail(p, MCBA_ERR_INVALID, "null argument");
-  const size_t before = p->hp.n_edges();
+  const size_t before = p->hp.n_edges(), ubefore = p->hp.u_Xw.size();
   if (first_id) *first_id = (int32_t)before;
   for (int32_t i = 0; i < n; ++i) {
     const float inf = info ? info[i] : 1.f;
@@ -573,7 +574,7 @@ int mcba_add_edges(mcba_problem* p, int32_t n, const uint8_t* type, const int32_
       h.e_delta.resize(before);
       h.e_robust.resize(before);
       h.e_level.resize(before);
-      h.e_Xw.resize(3 * before);
+      h.u_Xw.resize(ubefore);
       return r;
     }
   }
@@ -612,40 +613,53 @@ int mcba_load(mcba_problem* p, const mcba_problem_desc* d) {
     h.point_fixed[k] = d->point_fixed ? (d->point_fixed[k] ? 1 : 0) : 0;
   }
   const size_t E = d->n_edges;
-  h.e_type.resize(E);
-  h.e_pose.resize(E);
-  h.e_point.resize(E);
-  h.e_cam.resize(E);
-  h.e_obs.resize(3 * E);
-  h.e_info.resize(E);
-  h.e_delta.resize(E);
-  h.e_robust.resize(E);
-  h.e_level.resize(E);
-  h.e_Xw.assign(3 * E, 0.0);
   const int K = d->n_poses, P = d->n_points, C = d->n_cams;
+  // bulk copies, then one branch-free validation pass (the failing edge is
+  // looked up only when the pass reports a problem)
+  h.e_type.assign(d->edge_type, d->edge_type + E);
+  h.e_pose.assign(d->edge_pose, d->edge_pose + E);
+  h.e_point.assign(d->edge_point, d->edge_point + E);
+  h.e_cam.assign(d->edge_cam, d->edge_cam + E);
+  h.e_obs.assign(d->edge_obs, d->edge_obs + 3 * E);
+  if (d->edge_info) h.e_info.assign(d->edge_info, d->edge_info + E);
+  else h.e_info.assign(E, 1.f);
+  if (d->edge_delta) h.e_delta.assign(d->edge_delta, d->edge_delta + E);
+  else h.e_delta.assign(E, 0.f);
+  h.e_robust.resize(E);
+  if (d->edge_robust)
+    for (size_t i = 0; i < E; ++i) h.e_robust[i] = d->edge_robust[i] ? 1 : 0;
+  else
+    std::fill(h.e_robust.begin(), h.e_robust.end(), (uint8_t)1);
+  if (d->edge_level) h.e_level.assign(d->edge_level, d->edge_level + E);
+  else h.e_level.assign(E, 0);
+  auto nonfinite = [](float v) {
+    uint32_t b;
+    std::memcpy(&b, &v, 4);
+    return (b & 0x7f800000u) == 0x7f800000u;
+  };
+  unsigned bad_type = 0, bad_index = 0, bad_obs = 0, bad_w = 0;
+  size_t n_unary = 0;
   for (size_t i = 0; i < E; ++i) {
-    const uint8_t t = d->edge_type[i];
-    if (t > MCBA_EDGE_UNARY) return fail(p, MCBA_ERR_INVALID, "unknown edge type");
-    if (d->edge_pose[i] < 0 || d->edge_pose[i] >= K || d->edge_point[i] < 0 || d->edge_point[i] >= P ||
-        d->edge_cam[i] < 0 || d->edge_cam[i] >= C)
-      return fail(p, MCBA_ERR_INVALID, "edge index out of range");
-    h.e_type[i] = t;
-    h.e_pose[i] = d->edge_pose[i];
-    h.e_point[i] = t == MCBA_EDGE_UNARY ? -1 : d->edge_point[i];
-    h.e_cam[i] = d->edge_cam[i];
-    for (int a = 0; a < 3; ++a) {
-      const float v = d->edge_obs[3 * i + a];
-      if (!std::isfinite(v)) return fail(p, MCBA_ERR_NONFINITE, "non-finite observation");
-      h.e_obs[3 * i + a] = v;
-    }
-    h.e_info[i] = d->edge_info ? d->edge_info[i] : 1.f;
-    h.e_delta[i] = d->edge_delta ? d->edge_delta[i] : 0.f;
-    if (!std::isfinite(h.e_info[i]) || !std::isfinite(h.e_delta[i]))
-      return fail(p, MCBA_ERR_NONFINITE, "non-finite information or Huber threshold");
-    h.e_robust[i] = d->edge_robust ? (d->edge_robust[i] ? 1 : 0) : 1;
-    h.e_level[i] = d->edge_level ? d->edge_level[i] : 0;
-    if (t == MCBA_EDGE_UNARY)
-      for (int a = 0; a < 3; ++a) h.e_Xw[3 * i + a] = d->point_Xw[3 * (size_t)d->edge_point[i] + a];
+    const uint8_t t = h.e_type[i];
+    bad_type |= t > MCBA_EDGE_UNARY;
+    bad_index |= (unsigned)h.e_pose[i] >= (unsigned)K || (unsigned)h.e_point[i] >= (unsigned)P ||
+                 (unsigned)h.e_cam[i] >= (unsigned)C;
+    bad_obs |= nonfinite(h.e_obs[3 * i]) | nonfinite(h.e_obs[3 * i + 1]) | nonfinite(h.e_obs[3 * i + 2]);
+    bad_w |= nonfinite(h.e_info[i]) | nonfinite(h.e_delta[i]);
+    n_unary += t == MCBA_EDGE_UNARY;
+  }
+  if (bad_type) return fail(p, MCBA_ERR_INVALID, "unknown edge type");
+  if (bad_index) return fail(p, MCBA_ERR_INVALID, "edge index out of range");
+  if (bad_obs) return fail(p, MCBA_ERR_NONFINITE, "non-finite observation");
+  if (bad_w) return fail(p, MCBA_ERR_NONFINITE, "non-finite information or Huber threshold");
+  h.u_Xw.clear();
+  if (n_unary) {
+    h.u_Xw.reserve(3 * n_unary);
+    for (size_t i = 0; i < E; ++i)
+      if (h.e_type[i] == MCBA_EDGE_UNARY) {
+        for (int a = 0; a < 3; ++a) h.u_Xw.push_back(d->point_Xw[3 * (size_t)h.e_point[i] + a]);
+        h.e_point[i] = -1;
+      }
   }
   return MCBA_OK;
 }

@@ -38,7 +38,7 @@ struct HostProblem {
   std::vector<float> e_obs;  // [E][3]
   std::vector<float> e_info, e_delta;
   std::vector<uint8_t> e_robust, e_level;
-  std::vector<double> e_Xw;  // [E][3] constant point of unary edges (0 otherwise)
+  std::vector<double> u_Xw;  // [U][3] constant points of the unary edges, in edge order
 
   size_t n_edges() const { return e_type.size(); }
   void clear() {
@@ -56,7 +56,7 @@ struct HostProblem {
     e_delta.clear();
     e_robust.clear();
     e_level.clear();
-    e_Xw.clear();
+    u_Xw.clear();
   }
 };
 

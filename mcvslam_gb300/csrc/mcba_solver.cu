@@ -1186,14 +1186,7 @@ int upload_state(Solver* s, const HostProblem& hp, int U, int64_t& bytes, std::s
   }
   std::vector<double> X(3 * (size_t)(P + U) + 3, 0.0);
   std::copy(hp.points.begin(), hp.points.end(), X.begin());
-  {
-    int u = 0;
-    for (size_t i = 0; i < hp.n_edges(); ++i)
-      if (hp.e_type[i] == MCBA_EDGE_UNARY) {
-        for (int d = 0; d < 3; ++d) X[3 * (size_t)(P + u) + d] = hp.e_Xw[3 * i + d];
-        ++u;
-      }
-  }
+  std::copy(hp.u_Xw.begin(), hp.u_Xw.begin() + std::min<size_t>(hp.u_Xw.size(), 3 * (size_t)U), X.begin() + 3 * (size_t)P);
   std::vector<CamD> cd(hp.cams.size());
   std::vector<CamF> cf(hp.cams.size());
   for (size_t c = 0; c < hp.cams.size(); ++c) cam_to_dev(hp.cams[c], cd[c], cf[c]);
