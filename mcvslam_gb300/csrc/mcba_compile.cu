@@ -150,6 +150,15 @@ __global__ void __launch_bounds__(256) k_part_scatter(const int* keys, int n, in
   }
 }
 
+// atomicAdd(&c[k], 1) with one atomic per distinct key in the warp (callers
+// in a warp often hit the same few counters)
+__device__ __forceinline__ void count_warp(int* c, int k, bool on) {
+  const unsigned m = __ballot_sync(0xffffffffu, on);
+  if (!on) return;
+  const unsigned peers = __match_any_sync(m, k);
+  if ((peers & ((1u << (threadIdx.x & 31)) - 1u)) == 0) atomicAdd(&c[k], __popc(peers));
+}
+
 // ------------------------------------------------------ compile kernels --
 struct Raw {
   const int* pose;
@@ -201,18 +210,18 @@ __global__ void k_assign(const int* vact, const uint8_t* fixed, const int* scann
 __global__ void k_edge_index(Raw r, int E, int Kf, const int* act, const int* pose_h, const int* point_h, int* eph,
                              int* elh, int* pt_cnt, int* bucket_cnt, int* canon_cnt) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= E) return;
-  const int ph = pose_h[r.pose[i]];
-  const int lh = (r.type[i] == MCBA_EDGE_UNARY) ? -1 : point_h[r.point[i]];
-  eph[i] = ph;
-  elh[i] = lh;
-  if (!act[i]) return;
-  const int b = ph >= 0 ? ph : Kf;
-  atomicAdd(&bucket_cnt[b], 1);
-  if (lh >= 0) {
-    atomicAdd(&pt_cnt[lh], 1);
-    atomicAdd(&canon_cnt[b], 1);
+  const bool in = i < E;
+  const int ph = in ? pose_h[r.pose[i]] : -1;
+  const int lh = (!in || r.type[i] == MCBA_EDGE_UNARY) ? -1 : point_h[r.point[i]];
+  if (in) {
+    eph[i] = ph;
+    elh[i] = lh;
   }
+  const bool a = in && act[i];
+  const int b = ph >= 0 ? ph : Kf;
+  count_warp(bucket_cnt, b, a);
+  count_warp(canon_cnt, b, a && lh >= 0);
+  count_warp(pt_cnt, lh, a && lh >= 0);
 }
 
 __global__ void k_canon_fill(int E, const int* act, const int* elh, const int* pt_begin, int* fillc, int* canon_id) {
@@ -381,11 +390,30 @@ __global__ void k_block_ids(int Kf, const int* flag_scan, const int* present, in
   }
 }
 
+// pair counts per block: each thread counts its point's pairs per block in
+// a short local list first (a point has few distinct pose pairs), so the
+// global atomics are one per (point, block)
 __global__ void k_pair_block_count(int Lf, int Kf, const int* pt_begin, const int* cph, const int* blk_of,
                                    int* bcnt) {
   const int l = blockIdx.x * blockDim.x + threadIdx.x;
   if (l >= Lf) return;
-  visit_pairs(pt_begin[l], pt_begin[l + 1], cph, [&](int a, int b, int, int) { atomicAdd(&bcnt[blk_of[a * Kf + b]], 1); });
+  constexpr int kList = 8;
+  int key[kList] = {0}, cnt[kList] = {0}, n = 0;
+  visit_pairs(pt_begin[l], pt_begin[l + 1], cph, [&](int a, int b, int, int) {
+    const int k = blk_of[a * Kf + b];
+    int q = 0;
+    while (q < n && key[q] != k) ++q;
+    if (q < n) {
+      ++cnt[q];
+    } else if (n < kList) {
+      key[n] = k;
+      cnt[n] = 1;
+      ++n;
+    } else {
+      atomicAdd(&bcnt[k], 1);
+    }
+  });
+  for (int q = 0; q < n; ++q) atomicAdd(&bcnt[key[q]], cnt[q]);
 }
 
 __global__ void k_pchunk_count(int nblk, const int* bcnt, int* nch) {

@@ -60,6 +60,7 @@ struct LMState {
   int trial_continue, terminate, total_trials, n_log;
   int max_trials, max_log, last_accepted, max_iters;
   int outer_runs, pad0;
+  unsigned long long lam_bits;  // max |H_jj| as ordered IEEE bits (lambda init)
 };
 
 struct Bufs {
@@ -345,7 +346,8 @@ __global__ void k_point_reduce(Bufs B, int Lf, int n) {
 }
 
 // computeLambdaInit (optimization_algorithm_levenberg.cpp:145-157):
-// tau * max |H_jj| over every free vertex (poses and points).
+// tau * max |H_jj| over every free vertex (poses and points): a grid-wide
+// maximum (atomicMax on the bit pattern) and then the scaling.
 // |x| as an order-preserving integer: for non-negative doubles the IEEE bit
 // pattern orders like the value, so the maximum needs no FP64 instruction.
 __device__ __forceinline__ unsigned long long abs_bits(double x) {
@@ -353,18 +355,19 @@ __device__ __forceinline__ unsigned long long abs_bits(double x) {
 }
 
 template <typename R>
-__global__ void k_lambda_init(Bufs B, int Kf, int Lf, double tau) {
+__global__ void k_lambda_max(Bufs B, int Kf, int Lf) {
   __shared__ unsigned long long sh[32];
   if (B.lm->iteration != 0) return;
   unsigned long long m = 0;
-  for (int i = threadIdx.x; i < 6 * Kf; i += blockDim.x) {
-    const unsigned long long v = abs_bits(B.Hpp[(size_t)(i / 6) * 36 + 7 * (i % 6)]);
-    m = v > m ? v : m;
-  }
-  for (int i = threadIdx.x; i < 3 * Lf; i += blockDim.x) {
-    const int d = i % 3;
-    const unsigned long long v =
-        abs_bits((double)Ptrs<R>::p(B.Hll)[(size_t)(i / 3) * 6 + (d == 0 ? 0 : d == 1 ? 3 : 5)]);
+  const int n = 6 * Kf + 3 * Lf;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    unsigned long long v;
+    if (k < 6 * Kf) {
+      v = abs_bits(B.Hpp[(size_t)(k / 6) * 36 + 7 * (k % 6)]);
+    } else {
+      const int i = k - 6 * Kf, d = i % 3;
+      v = abs_bits((double)Ptrs<R>::p(B.Hll)[(size_t)(i / 3) * 6 + (d == 0 ? 0 : d == 1 ? 3 : 5)]);
+    }
     m = v > m ? v : m;
   }
 #pragma unroll
@@ -377,9 +380,14 @@ __global__ void k_lambda_init(Bufs B, int Kf, int Lf, double tau) {
   if (threadIdx.x == 0) {
     unsigned long long r = 0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = sh[w] > r ? sh[w] : r;
-    B.lm->lambda = tau * __longlong_as_double((long long)r);
-    B.lm->ni = 2.0;
+    atomicMax(&B.lm->lam_bits, r);
   }
+}
+
+__global__ void k_lambda_set(LMState* lm, double tau) {
+  if (lm->iteration != 0) return;
+  lm->lambda = tau * __longlong_as_double((long long)lm->lam_bits);
+  lm->ni = 2.0;
 }
 
 template <typename R>
@@ -1310,8 +1318,10 @@ void launch_linearize(Solver* s, const Bufs& B, const Launch& L, bool first, dou
       s->launches++;
     }
     if (first) {
-      k_lambda_init<R><<<1, 256, 0, st>>>(B, L.Kf, L.Lf, tau);
-      s->launches++;
+      const int nv = 6 * L.Kf + 3 * L.Lf;
+      k_lambda_max<R><<<std::max(1, std::min((nv + 255) / 256, 304)), 256, 0, st>>>(B, L.Kf, L.Lf);
+      k_lambda_set<<<1, 1, 0, st>>>(B.lm, tau);
+      s->launches += 2;
     }
   });
 }
