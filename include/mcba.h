@@ -265,6 +265,22 @@ int mcba_pose_optimization(mcba_problem* p, int32_t rounds, int32_t iterations, 
 int mcba_local_ba(mcba_problem* p, int32_t iterations, float chi2_threshold, int32_t* success_edges,
                   int32_t* written);
 
+/* ------------------------------------------- batched local-BA windows -- */
+/* Many independent local-BA windows solved together (the windows of config
+ * 4): PoseEstimation::BoundleAdjustment (include/PoseEstimation.hpp:36-119)
+ * on each window, with the n LM loops as independent branches of one CUDA
+ * graph launched once (no host round trip between windows or trials).
+ * mcba_batch_prepare compiles and uploads every handle's problem (as
+ * mcba_prepare); mcba_batch_solve restores each uploaded initial state and
+ * runs `iterations` LM iterations on all of them; mcba_fetch_state then
+ * reads one window's estimates back.  All handles must be on one device; the
+ * LM options (tau, max_trials) of problems[0] apply to the batch.  stats may
+ * be NULL, else it receives n entries; ms_device (may be NULL) the device
+ * time of the launch. */
+int mcba_batch_prepare(mcba_problem* const* problems, int32_t n);
+int mcba_batch_solve(mcba_problem* const* problems, int32_t n, int32_t iterations, mcba_stats* stats,
+                     double* ms_device);
+
 /* --------------------------------------------- batched pose-only solve -- */
 /* Many independent PoseEstimation::PoseOptimization problems
  * (src/PoseEstimation.cpp:48-130) of uneven size in one device pass: a

@@ -232,6 +232,42 @@ def batch_pose_only(problems, precision: str = "mixed", rounds: int = 4, iterati
             "ms_device": ms.value}
 
 
+class LocalBABatch:
+    """Many local-BA windows solved in one CUDA graph launch (mcba_batch_*)."""
+
+    def __init__(self, problems, precision: str = "mixed", device: int = 0):
+        self.solvers = [Solver(precision=precision, device=device).load(pr) for pr in problems]
+        self.L = N.lib()
+        arr = (ctypes.c_void_p * len(self.solvers))(*[s.h.value for s in self.solvers])
+        self._arr = arr
+        N.check(self.L.mcba_batch_prepare(arr, len(self.solvers)))
+
+    def solve(self, iterations: int = 10):
+        n = len(self.solvers)
+        stats = (N.Stats * n)()
+        ms = ctypes.c_double(0.0)
+        N.check(self.L.mcba_batch_solve(self._arr, n, iterations, stats, ctypes.byref(ms)), self.solvers[0].h)
+        return [st.as_dict() for st in stats], ms.value
+
+    def states(self):
+        out = []
+        for s in self.solvers:
+            s.fetch_state()
+            out.append(s.state())
+        return out
+
+    def close(self):
+        for s in self.solvers:
+            s.close()
+        self.solvers = []
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
 def solve(pr: synth.Problem, iterations: int = 10, precision: str = "fp64", **kw) -> dict:
     """Load, optimise and read back one problem; returns stats, state and trial log."""
     with Solver(precision=precision, **kw) as s:

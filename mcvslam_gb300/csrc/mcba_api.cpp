@@ -789,6 +789,42 @@ int mcba_prepare(mcba_problem* p) {
   return MCBA_OK;
 }
 
+int mcba_batch_prepare(mcba_problem* const* problems, int32_t n) {
+  if (n < 0 || (n > 0 && !problems)) return MCBA_ERR_INVALID;
+  for (int32_t i = 0; i < n; ++i) {
+    if (!problems[i]) return MCBA_ERR_INVALID;
+    const int r = mcba_prepare(problems[i]);
+    if (r) return r;
+  }
+  return MCBA_OK;
+}
+
+int mcba_batch_solve(mcba_problem* const* problems, int32_t n, int32_t iterations, mcba_stats* stats,
+                     double* ms_device) {
+  if (n < 0 || iterations < 0 || (n > 0 && !problems)) return MCBA_ERR_INVALID;
+  if (n == 0) return MCBA_OK;
+  std::vector<Solver*> ss(n);
+  for (int32_t i = 0; i < n; ++i) {
+    mcba_problem* p = problems[i];
+    if (!p) return MCBA_ERR_INVALID;
+    if (stats) std::memset(&stats[i], 0, sizeof(mcba_stats));
+    if (!p->prepared || !solver_has_upload(p->solver)) return fail(p, MCBA_ERR_INVALID, "mcba_batch_prepare first");
+    ss[i] = p->solver;
+  }
+  std::vector<SolveResult> res(n);
+  std::string e;
+  const int r = solver_run_batch(ss.data(), n, run_options(problems[0], iterations), res.data(), ms_device, &e);
+  for (int32_t i = 0; i < n; ++i) {
+    mcba_problem* p = problems[i];
+    p->log = res[i].log;
+    p->hpp = res[i].hpp;
+    p->hpp_kf = p->st.Kf;
+    if (stats) fill_stats(&stats[i], res[i], &p->st, r);
+  }
+  if (r) return fail(problems[0], r, e);
+  return MCBA_OK;
+}
+
 int mcba_solve_prepared(mcba_problem* p, int32_t iterations, mcba_stats* st) {
   if (!p || iterations < 0) return fail(p, MCBA_ERR_INVALID, "bad argument");
   if (st) std::memset(st, 0, sizeof(*st));

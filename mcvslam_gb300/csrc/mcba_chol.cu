@@ -356,7 +356,11 @@ __global__ void __launch_bounds__(kThreads) k_ldlt_cluster(const double* __restr
 
   // ---- backward solve L^T x = y (y: row 0 of the right-hand-side tiles) on
   //      CTA 0, which streams block row J-1 of L in while it works on row J
-  if (*flag0) {
+  // every CTA reads CTA 0's flag before any CTA may leave (a CTA's shared
+  // memory must not be read remotely once it has exited)
+  const int failed = *flag0;
+  cl.sync();
+  if (failed) {
     if (r == 0 && tid == 0) *solve_ok = 0;
     return;  // no CTA touches distributed shared memory after this point
   }

@@ -202,6 +202,11 @@ int solver_upload(Solver* s, const HostProblem& hp, const Structure* st, Structu
 // Runs LM on the uploaded problem; restore = start again from the uploaded
 // initial state.
 int solver_run(Solver* s, const RunOptions& o, bool restore, SolveResult& out, std::string* err);
+// LM on several uploaded problems at once: every solver's solve (restored
+// from its uploaded initial state) is a branch of one CUDA graph, launched
+// once.  ms_device: event time of that launch.
+int solver_run_batch(Solver* const* ss, int n, const RunOptions& o, SolveResult* outs, double* ms_device,
+                     std::string* err);
 // Copies the current device state into hp.
 int solver_download(Solver* s, HostProblem& hp, SolveResult& out, std::string* err);
 bool solver_has_upload(const Solver* s);

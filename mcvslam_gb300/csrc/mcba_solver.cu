@@ -31,6 +31,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -963,6 +964,7 @@ class Solver {
   bool uploaded = false;
   int64_t launches = 0;
   int generation = 0;
+  long long uid = 0;  // process-unique id (keys of cached batch graphs)
   // captured LM loop
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
@@ -1068,6 +1070,8 @@ Solver* solver_create(int device, int precision, void* stream, std::string* err)
       }
   }
   Solver* s = new Solver();
+  static std::atomic<long long> next_uid{1};
+  s->uid = next_uid++;
   s->device = device;
   s->precision = precision;
   if (stream) {
@@ -1446,16 +1450,17 @@ int capture_leaves(cudaStream_t st, std::vector<cudaGraphNode_t>& leaves, std::s
 //   while (iterate) { linearise; while (trial) { Schur, Cholesky, update,
 //   cost, decide }; end-of-iteration test }
 // with both loop conditions set on the device (k_lm_decide, k_iter_end).
+// Adds solver s's whole LM solve to graph G as an independent branch: the
+// prologue, then
+//   while (iterate) { linearise; while (trial) { Schur, Cholesky, update,
+//   cost, decide }; end-of-iteration test }
+// with both loop conditions set on the device (k_lm_decide, k_iter_end).
 template <typename R>
-int build_graph(Solver* s, const RunOptions& o, bool restore, std::string* err) {
-  s->graph_release();
+int add_lm_subgraph(Solver* s, cudaGraph_t G, const RunOptions& o, bool restore, std::string* err) {
   const Launch& L = s->L;
   const Bufs B = make_bufs(s);
   cudaStream_t st = s->stream;
   PhaseClock pc{s, false, {}};
-  cudaGraph_t G;
-  CK(cudaGraphCreate(&G, 0));
-  s->graph = G;
   cudaGraphConditionalHandle h_iter, h_trial;
   CK(cudaGraphConditionalHandleCreate(&h_iter, G, 0, cudaGraphCondAssignDefault));
   std::vector<cudaGraphNode_t> leaves;
@@ -1514,7 +1519,17 @@ int build_graph(Solver* s, const RunOptions& o, bool restore, std::string* err) 
   CK(cudaStreamEndCapture(st, &tmp));
   s->g_per_iter = (s->launches - l1) - s->g_per_trial;
   s->launches = l0;
+  return MCBA_OK;
+}
 
+template <typename R>
+int build_graph(Solver* s, const RunOptions& o, bool restore, std::string* err) {
+  s->graph_release();
+  cudaGraph_t G;
+  CK(cudaGraphCreate(&G, 0));
+  s->graph = G;
+  const int r = add_lm_subgraph<R>(s, G, o, restore, err);
+  if (r) return r;
   CK(cudaGraphInstantiate(&s->gexec, G, 0));
   s->g_gen = s->generation;
   s->g_iters = o.iterations;
@@ -1761,6 +1776,104 @@ int solver_upload(Solver* s, const HostProblem& hp, const Structure* hst, Struct
       s->g_sig.swap(sig);
       s->generation++;
     }
+  }
+  return MCBA_OK;
+}
+
+namespace {
+// The graph of the last batch solved (independent branches, one per solver),
+// kept while the same workspaces, uploads and options come back.
+struct BatchGraph {
+  std::vector<long long> uids;
+  std::vector<int> gens;
+  std::vector<const void*> logs;
+  int iters = -1, trials = -1, device = -1;
+  double tau = 0.0;
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t ge = nullptr;
+  int64_t launches_prologue = 0;
+  void release() {
+    if (ge) cudaGraphExecDestroy(ge);
+    if (g) cudaGraphDestroy(g);
+    ge = nullptr;
+    g = nullptr;
+    uids.clear();
+  }
+};
+std::mutex g_batch_mu;
+BatchGraph g_batch;
+}  // namespace
+
+int solver_run_batch(Solver* const* ss, int n, const RunOptions& o, SolveResult* outs, double* ms_device,
+                     std::string* err) {
+  if (n <= 0) return MCBA_OK;
+  for (int i = 0; i < n; ++i) {
+    if (!ss[i] || !ss[i]->uploaded) {
+      if (err) *err = "every problem of the batch must be prepared";
+      return MCBA_ERR_INVALID;
+    }
+    if (ss[i]->device != ss[0]->device) {
+      if (err) *err = "the problems of one batch must be on one device";
+      return MCBA_ERR_INVALID;
+    }
+  }
+  CK(cudaSetDevice(ss[0]->device));
+  const int max_log = std::max(1, o.iterations * o.max_trials);
+  for (int i = 0; i < n; ++i) CK(ss[i]->log.ensure(max_log));
+  std::lock_guard<std::mutex> lk(g_batch_mu);
+  std::vector<long long> uids(n);
+  std::vector<int> gens(n);
+  std::vector<const void*> logs(n);
+  for (int i = 0; i < n; ++i) {
+    uids[i] = ss[i]->uid;
+    gens[i] = ss[i]->generation;
+    logs[i] = ss[i]->log.p;
+  }
+  BatchGraph& bg = g_batch;
+  if (!bg.ge || bg.uids != uids || bg.gens != gens || bg.logs != logs || bg.iters != o.iterations ||
+      bg.trials != o.max_trials || bg.tau != o.tau || bg.device != ss[0]->device) {
+    bg.release();
+    CK(cudaGraphCreate(&bg.g, 0));
+    for (int i = 0; i < n; ++i) {
+      const int r = (ss[i]->precision == MCBA_PREC_MIXED) ? add_lm_subgraph<float>(ss[i], bg.g, o, true, err)
+                                                          : add_lm_subgraph<double>(ss[i], bg.g, o, true, err);
+      if (r) {
+        bg.release();
+        return r;
+      }
+    }
+    CK(cudaGraphInstantiate(&bg.ge, bg.g, 0));
+    bg.uids = uids;
+    bg.gens = gens;
+    bg.logs = logs;
+    bg.iters = o.iterations;
+    bg.trials = o.max_trials;
+    bg.tau = o.tau;
+    bg.device = ss[0]->device;
+  }
+  Solver* s0 = ss[0];
+  cudaStream_t stm = s0->stream;
+  CK(cudaEventRecord(s0->ev[0], stm));
+  CK(cudaGraphLaunch(bg.ge, stm));
+  CK(cudaEventRecord(s0->ev[1], stm));
+  for (int i = 0; i < n; ++i) {
+    CK(cudaMemcpyAsync(ss[i]->lm_host, ss[i]->lm.p, sizeof(LMState), cudaMemcpyDeviceToHost, stm));
+    outs[i].d2h += sizeof(LMState);
+  }
+  CK(cudaStreamSynchronize(stm));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, s0->ev[0], s0->ev[1]);
+  if (ms_device) *ms_device = ms;
+  for (int i = 0; i < n; ++i) {
+    Solver* s = ss[i];
+    SolveResult& out = outs[i];
+    out.ms_total = ms;
+    out.iterations = s->lm_host->iteration;
+    out.launches += s->g_prologue + s->g_per_iter * (int64_t)s->lm_host->iteration +
+                    s->g_per_trial * (int64_t)s->lm_host->total_trials;
+    const int r = (s->precision == MCBA_PREC_MIXED) ? finish_run<float>(s, o, out, err)
+                                                    : finish_run<double>(s, o, out, err);
+    if (r) return r;
   }
   return MCBA_OK;
 }

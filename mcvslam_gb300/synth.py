@@ -429,6 +429,19 @@ def random_edges(n: int, seed: int, rig: Optional[Rig] = None):
 
 
 # ------------------------------------------------------------ named configs --
+def window_batch(n: int = 64, seed: int = 4000, kf_range=(5, 40), pts_per_kf=(50, 300)) -> list:
+    """Local-BA windows of the batched benchmark: n windows of U(5, 40)
+    keyframes with U(50, 300) map points per keyframe (corridor layout, so
+    points follow the trajectory), 5% outliers, first 2 keyframes fixed."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for w in range(n):
+        k = int(rng.integers(kf_range[0], kf_range[1] + 1))
+        ppk = int(rng.integers(pts_per_kf[0], pts_per_kf[1] + 1))
+        out.append(local_ba(k, k * ppk, seed + 1 + w, corridor=True, name=f"window{w}_{k}kf"))
+    return out
+
+
 def config(idx: int, rep: int = 0) -> Problem:
     """Benchmark configurations (1-based, seed = idx * 1000 + rep).
 

@@ -51,3 +51,26 @@ def test_mixed_batch_of_uneven_problems(gpu):
         gt = p.gt_pose_Tcw[0]
         assert np.abs(mixed["pose_qt"][i][4:] - plain["pose_qt"][i][4:]).max() < 1e-4
     assert mixed["ms_device"] > 0
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_local_ba_windows_in_one_launch_equal_single_solves(precision, gpu):
+    """Windows solved as branches of one graph give exactly the single solves."""
+    wins = synth.window_batch(6, seed=77, kf_range=(5, 12), pts_per_kf=(50, 120))
+    single = []
+    for pr in wins:
+        with ba.Solver(precision=precision) as s:
+            s.load(pr)
+            st = s.optimize(6)
+            single.append((st, s.trial_log(), s.state()))
+    with ba.LocalBABatch(wins, precision=precision) as b:
+        for rep in range(2):  # the second run reuses the cached batch graph
+            stats, ms = b.solve(6)
+            assert ms > 0
+            states = b.states()
+            for (st, log, (qt, X)), bst, (bqt, bX), s in zip(single, stats, states, b.solvers):
+                assert bst["final_chi2"] == st["final_chi2"]
+                assert bst["iterations"] == st["iterations"] and bst["trials"] == st["trials"]
+                np.testing.assert_array_equal(s.trial_log(), log)
+                np.testing.assert_array_equal(bqt, qt)
+                np.testing.assert_array_equal(bX, X)

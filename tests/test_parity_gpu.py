@@ -256,3 +256,25 @@ def test_cached_workspaces_give_identical_solves(gpu):
         np.testing.assert_array_equal(other[1], first[1])
         np.testing.assert_array_equal(other[2][0], first[2][0])
         np.testing.assert_array_equal(other[2][1], first[2][1])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_indefinite_reduced_system_follows_oracle(precision, gpu):
+    """Every edge of one free keyframe carries a negative information weight,
+    so the reduced camera system is indefinite until the damping outgrows it:
+    the first trials' factorisations meet a negative pivot (g2o's solve() ==
+    false, chi2_new = DBL_MAX) and are rejected, then the growing lambda makes
+    the system positive definite and the solve proceeds -- trial by trial as
+    the oracle (FP64), with the same accept/fail pattern (mixed)."""
+    pr = synth.config(1)
+    pr.edge_info[pr.edge_pose == 5] = -1.0
+    o = oracle.optimize(pr, 3)
+    with ba.Solver(precision=precision) as s:
+        s.load(pr)
+        s.optimize(3)
+        log = s.trial_log()
+    assert (~o["log"]["solve_ok"].astype(bool)).sum() >= 3
+    np.testing.assert_array_equal(log["solve_ok"], o["log"]["solve_ok"])
+    np.testing.assert_array_equal(log["accepted"], o["log"]["accepted"])
+    if precision == "fp64":
+        compare_logs(log, o["log"])
