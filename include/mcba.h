@@ -265,6 +265,25 @@ int mcba_pose_optimization(mcba_problem* p, int32_t rounds, int32_t iterations, 
 int mcba_local_ba(mcba_problem* p, int32_t iterations, float chi2_threshold, int32_t* success_edges,
                   int32_t* written);
 
+/* ---------------------------------------------- Hamming k = 2 matching -- */
+/* Matcher::KnnMatch over descriptor lists (src/Matcher.cpp:245-302): for
+ * each of nq 32-byte query descriptors, the best and second-best of nt train
+ * descriptors by Hamming distance (HammingDistance, include/Matcher.hpp:19-31),
+ * ties to the smaller train index, unfilled slots (999, 0) as the reference
+ * initialises them.  idx and dist receive [nq][2].  keep (may be NULL)
+ * receives FilterRatio(ratio) && FilterThreshold(max_dist) per query, the
+ * filters the callers apply (src/Matcher.cpp:23-34,100-111; the reference's
+ * defaults are 0.6 and 46).
+ * mcba_knn_hamming_device: device pointers (query and train 16-byte
+ * aligned), on `stream`; its chunk scratch is cached per device, so calls that
+ * may overlap on one device must be serialised by the caller.
+ * mcba_knn_hamming: host buffers, copies in and out inside the call;
+ * *ms_device (may be NULL) receives the kernel time. */
+int mcba_knn_hamming_device(const uint8_t* query, int32_t nq, const uint8_t* train, int32_t nt, int32_t* idx,
+                            int32_t* dist, float ratio, int32_t max_dist, uint8_t* keep, void* stream);
+int mcba_knn_hamming(int32_t device, const uint8_t* query, int32_t nq, const uint8_t* train, int32_t nt,
+                     int32_t* idx, int32_t* dist, float ratio, int32_t max_dist, uint8_t* keep, double* ms_device);
+
 /* ------------------------------------------- batched local-BA windows -- */
 /* Many independent local-BA windows solved together (the windows of config
  * 4): PoseEstimation::BoundleAdjustment (include/PoseEstimation.hpp:36-119)

@@ -123,6 +123,9 @@ def _declare(L):
         "mcba_batch_pose_only": ([i32, i32, i32, c_i32_p, i32, c_float_p, c_float_p, c_i32_p, c_float_p, c_float_p,
                                   c_float_p, c_float_p, i32, i32, ctypes.c_float, i32, c_double_p, c_u8_p, c_i32_p,
                                   c_double_p], ctypes.c_int),
+        "mcba_knn_hamming_device": ([P, i32, P, i32, P, P, ctypes.c_float, i32, P, P], ctypes.c_int),
+        "mcba_knn_hamming": ([i32, c_u8_p, i32, c_u8_p, i32, c_i32_p, c_i32_p, ctypes.c_float, i32, c_u8_p,
+                              c_double_p], ctypes.c_int),
         "mcba_robust_cost_noalloc": ([ctypes.c_int64, P, P, P, P, P, P, P, P, P, P], ctypes.c_int),
     }
     for name, (args, res) in sig.items():

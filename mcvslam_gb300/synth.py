@@ -460,3 +460,24 @@ def config(idx: int, rep: int = 0) -> Problem:
 
 # box placement that gives the configurations' edge counts (~9k / ~150k / ~2M)
 CONFIG_BOX_OFFSET = {1: -4.0, 2: 0.0, 5: 0.0}
+
+
+def descriptors(nq: int, nt: int, seed: int, match_frac: float = 0.6, flips: tuple = (0, 40)):
+    """ORB-like 32-byte descriptor sets for the matcher: nt random train
+    descriptors, and nq queries of which a fraction are copies of a random
+    train descriptor with a uniform number of bits in [flips) flipped (a
+    re-observation), the rest unrelated."""
+    rng = np.random.default_rng(seed)
+    train = rng.integers(0, 256, size=(nt, 32), dtype=np.uint8)
+    query = rng.integers(0, 256, size=(nq, 32), dtype=np.uint8)
+    if nt:
+        m = rng.random(nq) < match_frac
+        src = rng.integers(0, nt, size=nq)
+        bits = np.unpackbits(train[src], axis=1)
+        nflip = rng.integers(flips[0], flips[1], size=nq)
+        for i in np.nonzero(m)[0]:
+            b = bits[i].copy()
+            pos = rng.choice(256, size=int(nflip[i]), replace=False)
+            b[pos] ^= 1
+            query[i] = np.packbits(b)
+    return query, train

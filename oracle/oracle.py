@@ -72,6 +72,9 @@ def lib(threads: bool = False):
         L.orc_linearize_edges.argtypes = [ctypes.POINTER(OrcProblem), c_double_p, c_double_p, c_double_p]
         L.orc_normal_equations.argtypes = [ctypes.POINTER(OrcProblem), ctypes.c_double, c_double_p, c_double_p,
                                            c_double_p, ctypes.c_int]
+        L.orc_knn_hamming.argtypes = [c_u8_p, ctypes.c_int32, c_u8_p, ctypes.c_int32, c_i32_p, c_i32_p, ctypes.c_float,
+                                      ctypes.c_int32, c_u8_p, ctypes.c_int32]
+        L.orc_knn_hamming.restype = None
         for fn in ("orc_se3_exp", "orc_mat44f_to_qt", "orc_qt_to_mat44f", "orc_huber", "orc_compose", "orc_map"):
             getattr(L, fn).restype = None
         _LIBS[name] = L
@@ -243,3 +246,17 @@ def map_point(qt, X) -> np.ndarray:
     o = np.zeros(3)
     lib().orc_map(_ptr(qt, c_double_p), _ptr(X, c_double_p), _ptr(o, c_double_p))
     return o
+
+
+def knn_hamming(query, train, ratio: float = 0.6, max_dist: int = 46, n_threads: int = 1):
+    """Matcher::KnnMatch (k = 2) over 32-byte descriptors: [nq, 2] train
+    indices and distances plus the FilterRatio/FilterThreshold keep flag."""
+    q = np.ascontiguousarray(query, np.uint8).reshape(-1, 32)
+    t = np.ascontiguousarray(train, np.uint8).reshape(-1, 32)
+    nq, nt = q.shape[0], t.shape[0]
+    idx = np.zeros((nq, 2), np.int32)
+    dist = np.zeros((nq, 2), np.int32)
+    keep = np.zeros(nq, np.uint8)
+    lib(n_threads > 1).orc_knn_hamming(_ptr(q, c_u8_p), nq, _ptr(t, c_u8_p), nt, _ptr(idx, c_i32_p),
+                                        _ptr(dist, c_i32_p), ratio, max_dist, _ptr(keep, c_u8_p), n_threads)
+    return idx, dist, keep
