@@ -284,6 +284,57 @@ int mcba_knn_hamming_device(const uint8_t* query, int32_t nq, const uint8_t* tra
 int mcba_knn_hamming(int32_t device, const uint8_t* query, int32_t nq, const uint8_t* train, int32_t nt,
                      int32_t* idx, int32_t* dist, float ratio, int32_t max_dist, uint8_t* keep, double* ms_device);
 
+/* ------------------------------- map-point projection + windowed match -- */
+/* Object::ProjectBunchMapPoints (src/Object.cpp:208-236) for a batch of
+ * objects (one camera of one frame each; Tracker.cpp:90-91,128-129 make two
+ * such calls per frame).  For every map point of an object, in visit order:
+ * project with the object's pose and pinhole camera (R * X + t, then
+ * Pinhole::project, modules/camera/Pinhole.cpp:45-47), gather the keypoints
+ * of the 30 x 30 grid within r_threshold * mvScaleFactor[level] of the
+ * projection (GetFeaturesInArea, src/Object.cpp:263-300), k = 2 Hamming match
+ * of the map point's descriptor against them, FilterRatio(ratio) and
+ * FilterThreshold(max_dist) (src/Object.cpp:226; the reference passes the
+ * defaults 0.6 and 46), and bind the best keypoint (AddMapPoint,
+ * src/Object.cpp:113-137). */
+typedef struct mcba_projection_batch {
+  int32_t n_objects;
+  const float* obj_Rt;       /* [n_objects][12] camera from world: R row-major, then t */
+  const float* obj_K;        /* [n_objects][4] fx fy cx cy */
+  const int32_t* obj_size;   /* [n_objects][2] image cols, rows */
+  const float* obj_radius;   /* [n_objects] r_threshold */
+  const float* obj_scale;    /* [n_objects][n_levels] mvScaleFactor of the object's extractor */
+  int32_t n_levels;
+  float ratio;               /* FilterRatio */
+  int32_t max_dist;          /* FilterThreshold */
+  const int32_t* kp_begin;   /* [n_objects + 1] keypoint ranges, kp_begin[0] = 0 */
+  const float* kp_xy;        /* [n_kp][2] keypoint pixel position */
+  const uint8_t* kp_desc;    /* [n_kp][32] keypoint descriptors */
+  const int32_t* mp_begin;   /* [n_objects + 1] map-point ranges, in visit order, mp_begin[0] = 0 */
+  const float* mp_X;         /* [n_mp][3] world position */
+  const uint8_t* mp_desc;    /* [n_mp][32] MapPoint::GetDesp */
+  const int32_t* mp_level;   /* [n_mp] MapPoint::level, in [0, n_levels) */
+  const int32_t* mp_id;      /* [n_mp] the caller's handle, written into kp_bind */
+  const int32_t* mp_prev_kp; /* [n_mp] object-local keypoint the map point is bound to before the call
+                                (Object::mMP2IDX), or -1; NULL = none bound */
+} mcba_projection_batch;
+
+/* Host buffers.  kp_bind [n_kp] (in/out) holds each keypoint's bound map-point
+ * handle or -1 (Object::mIDX2MP) and is updated as the reference's sequence of
+ * AddMapPoint calls leaves it; mp_match [n_mp] receives the object-local
+ * keypoint each map point matched or -1 (its ProjectResRecord flag);
+ * obj_count [n_objects] the returned counts.  *ms_device (may be NULL): kernel
+ * time.  Invalid levels, ranges or non-finite inputs are errors. */
+int mcba_project_match(int32_t device, const mcba_projection_batch* batch, int32_t* kp_bind, int32_t* mp_match,
+                       int32_t* obj_count, double* ms_device);
+/* The same with every pointer in *batch and the outputs in device memory
+ * (kp_desc and mp_desc 16-byte aligned, kp_xy 8-byte aligned), on `stream`;
+ * n_kp = kp_begin[n_objects], n_mp = mp_begin[n_objects].  The contents are
+ * not validated (out-of-range levels or keypoints give no match); the grid
+ * scratch is cached per device, so overlapping calls on one device must be
+ * serialised by the caller. */
+int mcba_project_match_device(const mcba_projection_batch* batch, int32_t n_kp, int32_t n_mp, int32_t* kp_bind,
+                              int32_t* mp_match, int32_t* obj_count, void* stream);
+
 /* ------------------------------------------- batched local-BA windows -- */
 /* Many independent local-BA windows solved together (the windows of config
  * 4): PoseEstimation::BoundleAdjustment (include/PoseEstimation.hpp:36-119)

@@ -68,6 +68,18 @@ class ProblemDesc(ctypes.Structure):
     ]
 
 
+class ProjectionBatchDesc(ctypes.Structure):
+    """mcba_projection_batch; pointer fields as plain addresses (host or device)."""
+    _fields_ = [
+        ("n_objects", ctypes.c_int32), ("obj_Rt", ctypes.c_void_p), ("obj_K", ctypes.c_void_p),
+        ("obj_size", ctypes.c_void_p), ("obj_radius", ctypes.c_void_p), ("obj_scale", ctypes.c_void_p),
+        ("n_levels", ctypes.c_int32), ("ratio", ctypes.c_float), ("max_dist", ctypes.c_int32),
+        ("kp_begin", ctypes.c_void_p), ("kp_xy", ctypes.c_void_p), ("kp_desc", ctypes.c_void_p),
+        ("mp_begin", ctypes.c_void_p), ("mp_X", ctypes.c_void_p), ("mp_desc", ctypes.c_void_p),
+        ("mp_level", ctypes.c_void_p), ("mp_id", ctypes.c_void_p), ("mp_prev_kp", ctypes.c_void_p),
+    ]
+
+
 _LIB = None
 
 
@@ -126,6 +138,8 @@ def _declare(L):
         "mcba_knn_hamming_device": ([P, i32, P, i32, P, P, ctypes.c_float, i32, P, P], ctypes.c_int),
         "mcba_knn_hamming": ([i32, c_u8_p, i32, c_u8_p, i32, c_i32_p, c_i32_p, ctypes.c_float, i32, c_u8_p,
                               c_double_p], ctypes.c_int),
+        "mcba_project_match": ([i32, ctypes.POINTER(ProjectionBatchDesc), P, P, P, c_double_p], ctypes.c_int),
+        "mcba_project_match_device": ([ctypes.POINTER(ProjectionBatchDesc), i32, i32, P, P, P, P], ctypes.c_int),
         "mcba_robust_cost_noalloc": ([ctypes.c_int64, P, P, P, P, P, P, P, P, P, P], ctypes.c_int),
     }
     for name, (args, res) in sig.items():

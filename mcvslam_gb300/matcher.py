@@ -46,3 +46,77 @@ def knn_hamming_device(query, train, ratio: float = 0.6, max_dist: int = 46):
     N.check(N.lib().mcba_knn_hamming_device(q.data_ptr(), nq, t.data_ptr(), nt, idx.data_ptr(), dist.data_ptr(),
                                             ratio, max_dist, keep.data_ptr(), stream))
     return idx, dist, keep
+
+
+_PB_FIELDS = [("obj_Rt", "float32"), ("obj_K", "float32"), ("obj_size", "int32"), ("obj_radius", "float32"),
+              ("obj_scale", "float32"), ("kp_begin", "int32"), ("kp_xy", "float32"), ("kp_desc", "uint8"),
+              ("mp_begin", "int32"), ("mp_X", "float32"), ("mp_desc", "uint8"), ("mp_level", "int32"),
+              ("mp_id", "int32"), ("mp_prev_kp", "int32")]
+
+
+def _batch_desc(b, arrays):
+    d = N.ProjectionBatchDesc()
+    d.n_objects = b.n_objects
+    d.n_levels = int(b.obj_scale.shape[1])
+    d.ratio = float(b.ratio)
+    d.max_dist = int(b.max_dist)
+    for name, _ in _PB_FIELDS:
+        a = arrays.get(name)
+        setattr(d, name, None if a is None else (a.data_ptr() if hasattr(a, "data_ptr") else a.ctypes.data))
+    return d
+
+
+def project_match(b, device: int = 0):
+    """Object::ProjectBunchMapPoints over a batch of objects (host arrays of a
+    synth.ProjectionBatch-like object): (kp_bind after the call, mp_match,
+    obj_count, kernel ms)."""
+    arrays = {}
+    for name, dt in _PB_FIELDS:
+        v = getattr(b, name, None)
+        arrays[name] = None if v is None else np.ascontiguousarray(v, dtype=dt)
+    d = _batch_desc(b, arrays)
+    nk, nm = int(b.kp_begin[-1]), int(b.mp_begin[-1])
+    kp_bind = np.array(b.kp_bind, np.int32, copy=True)
+    mp_match = np.zeros(nm, np.int32)
+    count = np.zeros(b.n_objects, np.int32)
+    ms = ctypes.c_double(0.0)
+    N.check(N.lib().mcba_project_match(device, ctypes.byref(d), kp_bind.ctypes.data, mp_match.ctypes.data,
+                                       count.ctypes.data, ctypes.byref(ms)))
+    return kp_bind, mp_match, count, ms.value
+
+
+class DeviceProjectionBatch:
+    """A projection batch resident on the GPU (torch tensors), for repeated
+    device-side calls without host copies."""
+
+    def __init__(self, b, device: int = 0):
+        import torch
+
+        self.b = b
+        self.dev = torch.device("cuda", device)
+        self.t = {}
+        for name, dt in _PB_FIELDS:
+            v = getattr(b, name, None)
+            if v is not None:
+                self.t[name] = torch.from_numpy(np.ascontiguousarray(v, dtype=dt)).to(self.dev)
+        self.kp_bind0 = torch.from_numpy(np.ascontiguousarray(b.kp_bind, np.int32)).to(self.dev)
+        self.kp_bind = self.kp_bind0.clone()
+        self.nk, self.nm = int(b.kp_begin[-1]), int(b.mp_begin[-1])
+        self.mp_match = torch.empty(max(self.nm, 1), dtype=torch.int32, device=self.dev)
+        self.count = torch.empty(max(b.n_objects, 1), dtype=torch.int32, device=self.dev)
+        self.desc = _batch_desc(b, self.t)
+
+    def reset(self):
+        """Restore the bindings the batch started with (the call updates them in place)."""
+        self.kp_bind.copy_(self.kp_bind0)
+
+    def run(self, reset: bool = True):
+        """One call on torch's current stream; reset restores the initial bindings first."""
+        import torch
+
+        if reset:
+            self.reset()
+        stream = torch.cuda.current_stream(self.dev).cuda_stream
+        N.check(N.lib().mcba_project_match_device(ctypes.byref(self.desc), self.nk, self.nm, self.kp_bind.data_ptr(),
+                                                  self.mp_match.data_ptr(), self.count.data_ptr(), stream))
+        return self.kp_bind, self.mp_match[:self.nm], self.count[:self.b.n_objects]

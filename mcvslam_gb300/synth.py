@@ -481,3 +481,130 @@ def descriptors(nq: int, nt: int, seed: int, match_frac: float = 0.6, flips: tup
             b[pos] ^= 1
             query[i] = np.packbits(b)
     return query, train
+
+
+@dataclasses.dataclass
+class ProjectionBatch:
+    """Objects (one camera of one frame each) for Object::ProjectBunchMapPoints."""
+    obj_Rt: np.ndarray      # [O, 12] float32: R row-major then t (camera from world)
+    obj_K: np.ndarray       # [O, 4] float32
+    obj_size: np.ndarray    # [O, 2] int32 cols, rows
+    obj_radius: np.ndarray  # [O] float32
+    obj_scale: np.ndarray   # [O, L] float32
+    ratio: float
+    max_dist: int
+    kp_begin: np.ndarray    # [O+1] int32
+    kp_xy: np.ndarray       # [NK, 2] float32
+    kp_desc: np.ndarray     # [NK, 32] uint8
+    kp_bind: np.ndarray     # [NK] int32 (map-point id or -1)
+    mp_begin: np.ndarray    # [O+1] int32
+    mp_X: np.ndarray        # [NM, 3] float32
+    mp_desc: np.ndarray     # [NM, 32] uint8
+    mp_level: np.ndarray    # [NM] int32
+    mp_id: np.ndarray       # [NM] int32
+    mp_prev_kp: np.ndarray  # [NM] int32 (object-local keypoint already bound to the map point, or -1)
+
+    @property
+    def n_objects(self):
+        return int(self.obj_Rt.shape[0])
+
+
+def scale_factors(n_levels: int = 8, factor: float = 1.2) -> np.ndarray:
+    """ORB pyramid scale factors as ORBextractor fills mvScaleFactor (float,
+    each level the previous times the double factor)."""
+    s = np.zeros(n_levels, np.float32)
+    s[0] = 1.0
+    for i in range(1, n_levels):
+        s[i] = np.float32(float(s[i - 1]) * factor)
+    return s
+
+
+def projection_batch(n_objects: int, n_kp: int, n_mp: int, seed: int, radius: float = 10.0,
+                     rig: Optional[Rig] = None, observed_frac: float = 0.7, prebound_frac: float = 0.2,
+                     dup_frac: float = 0.05) -> ProjectionBatch:
+    """Each object: a camera looking down +z from a random pose near the origin,
+    n_mp map points in front of it (a few behind it or outside the image),
+    n_kp keypoints of which observed_frac of the map points leave one near
+    their projection with a perturbed descriptor, the rest clutter.  Some
+    keypoints start bound (to earlier map points, and to map points of this
+    call, with mp_prev_kp consistent); dup_frac of the map points repeat
+    another's descriptor and position, so several map points can claim one
+    keypoint."""
+    rng = np.random.default_rng(seed)
+    rig = rig or reference_rig()
+    O = n_objects
+    cams = rng.integers(0, rig.K.shape[0], size=O)
+    K = rig.K[cams].astype(np.float32)
+    size = rig.size[cams].astype(np.int32)
+    # small rotations only: cameras look roughly along +z
+    w = rng.normal(0, 0.05, size=(O, 3))
+    R = np.stack([so3_exp(wi) for wi in w])
+    t = rng.normal(0, 0.2, size=(O, 3))
+    Rt = np.concatenate([R.reshape(O, 9), t], axis=1).astype(np.float32)
+    scale = np.tile(scale_factors(), (O, 1))
+    kp_begin = np.arange(O + 1, dtype=np.int32) * n_kp
+    mp_begin = np.arange(O + 1, dtype=np.int32) * n_mp
+    kp_xy = np.zeros((O * n_kp, 2), np.float32)
+    kp_desc = rng.integers(0, 256, size=(O * n_kp, 32), dtype=np.uint8)
+    kp_bind = np.full(O * n_kp, -1, np.int32)
+    mp_X = np.zeros((O * n_mp, 3), np.float32)
+    mp_desc = rng.integers(0, 256, size=(O * n_mp, 32), dtype=np.uint8)
+    mp_level = rng.integers(0, 8, size=O * n_mp).astype(np.int32)
+    mp_id = (np.arange(O * n_mp, dtype=np.int64) * 7 + 1000).astype(np.int32)
+    mp_prev = np.full(O * n_mp, -1, np.int32)
+    next_free_id = int(mp_id.max()) + 1
+    for o in range(O):
+        cols, rows = int(size[o, 0]), int(size[o, 1])
+        fx, fy, cx, cy = [float(v) for v in K[o]]
+        # pixels and depths -> camera points -> world points
+        u = rng.uniform(-0.05 * cols, 1.05 * cols, n_mp)
+        v = rng.uniform(-0.05 * rows, 1.05 * rows, n_mp)
+        z = rng.uniform(2.0, 30.0, n_mp)
+        z[rng.random(n_mp) < 0.03] *= -1.0
+        Pc = np.stack([(u - cx) / fx * z, (v - cy) / fy * z, z], axis=1)
+        Xw = (Pc - t[o]) @ R[o]
+        mX = mp_X[o * n_mp:(o + 1) * n_mp]
+        mX[:] = Xw.astype(np.float32)
+        md = mp_desc[o * n_mp:(o + 1) * n_mp]
+        ml = mp_level[o * n_mp:(o + 1) * n_mp]
+        ndup = int(dup_frac * n_mp)
+        if ndup and n_mp > 1:
+            src = rng.integers(0, n_mp, ndup)
+            dst = rng.integers(0, n_mp, ndup)
+            mX[dst] = mX[src]
+            md[dst] = md[src]
+            ml[dst] = ml[src]
+        # keypoints: observations of map points, then clutter
+        kx = kp_xy[o * n_kp:(o + 1) * n_kp]
+        kd = kp_desc[o * n_kp:(o + 1) * n_kp]
+        kx[:, 0] = rng.uniform(0, cols, n_kp)
+        kx[:, 1] = rng.uniform(0, rows, n_kp)
+        obs = np.nonzero(rng.random(n_mp) < observed_frac)[0][:n_kp]
+        slots = rng.permutation(n_kp)[:obs.size]
+        Xc = mX[obs].astype(np.float64) @ R[o].T + t[o]
+        with np.errstate(divide="ignore", invalid="ignore"):
+            pu = fx * Xc[:, 0] / Xc[:, 2] + cx
+            pv = fy * Xc[:, 1] / Xc[:, 2] + cy
+        ok = np.isfinite(pu) & np.isfinite(pv)
+        kx[slots[ok], 0] = (pu[ok] + rng.normal(0, 1.5, ok.sum())).astype(np.float32)
+        kx[slots[ok], 1] = (pv[ok] + rng.normal(0, 1.5, ok.sum())).astype(np.float32)
+        bits = np.unpackbits(md[obs[ok]], axis=1)
+        flips = rng.random(bits.shape) < rng.uniform(0.0, 0.15, size=(bits.shape[0], 1))
+        kd[slots[ok]] = np.packbits(bits ^ flips.astype(np.uint8), axis=1)
+        # pre-existing bindings: a few to foreign map points, a few to map points of this call
+        kb = kp_bind[o * n_kp:(o + 1) * n_kp]
+        mpv = mp_prev[o * n_mp:(o + 1) * n_mp]
+        nb = int(prebound_frac * n_kp)
+        free = rng.permutation(n_kp)[:nb]
+        half = nb // 2
+        for i in free[:half]:
+            kb[i] = next_free_id
+            next_free_id += 1
+        own = rng.permutation(n_mp)[:nb - half]
+        for i, m in zip(free[half:], own):
+            kb[i] = mp_id[o * n_mp + m]
+            mpv[m] = i
+    return ProjectionBatch(obj_Rt=Rt, obj_K=K, obj_size=size, obj_radius=np.full(O, radius, np.float32),
+                           obj_scale=scale.astype(np.float32), ratio=0.6, max_dist=46, kp_begin=kp_begin,
+                           kp_xy=kp_xy, kp_desc=kp_desc, kp_bind=kp_bind, mp_begin=mp_begin, mp_X=mp_X,
+                           mp_desc=mp_desc, mp_level=mp_level, mp_id=mp_id, mp_prev_kp=mp_prev)

@@ -260,3 +260,30 @@ def knn_hamming(query, train, ratio: float = 0.6, max_dist: int = 46, n_threads:
     lib(n_threads > 1).orc_knn_hamming(_ptr(q, c_u8_p), nq, _ptr(t, c_u8_p), nt, _ptr(idx, c_i32_p),
                                         _ptr(dist, c_i32_p), ratio, max_dist, _ptr(keep, c_u8_p), n_threads)
     return idx, dist, keep
+
+
+def project_match(b, n_threads: int = 1):
+    """Object::ProjectBunchMapPoints over a synth.ProjectionBatch: (kp_bind
+    after the call, mp_match, obj_count)."""
+    L = lib(n_threads > 1)
+    c_f, c_i, c_u8 = c_float_p, c_i32_p, c_u8_p
+    if not hasattr(L, "_pm_sig"):
+        L.orc_project_match.argtypes = [ctypes.c_int32, ctypes.c_int32, c_f, c_f, c_i, c_f, c_f, ctypes.c_int32, ctypes.c_float,
+                                        ctypes.c_int32, c_i, c_f, c_u8, c_i, c_f, c_u8, c_i, c_i, c_i, c_i, c_i]
+        L.orc_project_match.restype = None
+        L._pm_sig = True
+    a = lambda x, dt: np.ascontiguousarray(x, dt)  # noqa: E731
+    keep = [a(b.obj_Rt, np.float32), a(b.obj_K, np.float32), a(b.obj_size, np.int32), a(b.obj_radius, np.float32),
+            a(b.obj_scale, np.float32), a(b.kp_begin, np.int32), a(b.kp_xy, np.float32), a(b.kp_desc, np.uint8),
+            a(b.mp_begin, np.int32), a(b.mp_X, np.float32), a(b.mp_desc, np.uint8), a(b.mp_level, np.int32),
+            a(b.mp_id, np.int32)]
+    kp_bind = np.array(b.kp_bind, np.int32, copy=True)
+    nm = int(b.mp_begin[-1])
+    mp_match = np.zeros(nm, np.int32)
+    obj_count = np.zeros(b.n_objects, np.int32)
+    ts = [c_f, c_f, c_i, c_f, c_f, c_i, c_f, c_u8, c_i, c_f, c_u8, c_i, c_i]
+    p = [_ptr(x, t) for x, t in zip(keep, ts)]
+    L.orc_project_match(n_threads, b.n_objects, p[0], p[1], p[2], p[3], p[4], int(b.obj_scale.shape[1]), b.ratio, b.max_dist,
+                        p[5], p[6], p[7], p[8], p[9], p[10], p[11], p[12], _ptr(kp_bind, c_i), _ptr(mp_match, c_i),
+                        _ptr(obj_count, c_i))
+    return kp_bind, mp_match, obj_count
