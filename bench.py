@@ -49,9 +49,11 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="ba", choices=["ba", "knn", "project"],
+    ap.add_argument("--workload", default="ba", choices=["ba", "knn", "project", "stereo"],
                     help="ba: the local-BA solve (default); knn: brute-force Hamming k=2 matching; "
-                         "project: map-point projection + windowed match over a batch of objects")
+                         "project: map-point projection + windowed match over a batch of objects; "
+                         "stereo: stereo matching of a batch of rectified frames")
+    ap.add_argument("--frames", type=int, default=256, help="stereo frames for --workload stereo")
     ap.add_argument("--objects", type=int, default=512, help="objects (frame cameras) for --workload project")
     ap.add_argument("--knn-n", type=int, default=32768, help="query and train descriptors for --workload knn")
     return ap.parse_args()
@@ -658,9 +660,130 @@ def run_project_reference(args):
     print(json.dumps(line), flush=True)
 
 
+STEREO_LEFT, STEREO_CLUTTER = 1500, 500  # left keypoints and unmatched right keypoints per frame
+
+
+def run_stereo(args):
+    """Frame::ComputeStereoMatch over args.frames rectified 512 x 512 frames
+    (8-level pyramids, 1500 left keypoints, ~1200 true right counterparts plus
+    500 clutter keypoints each), all in one call.  value = frames per second
+    with the batch resident; e2e = the host-buffer C entry (pyramids and
+    keypoints copied in, u_right/depth copied out)."""
+    import torch
+
+    from mcvslam_gb300 import matcher, synth
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    sb = synth.stereo_batch(args.frames, STEREO_LEFT, STEREO_CLUTTER, 7100)
+    db = matcher.DeviceStereoBatch(sb, device=local)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        db.run()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for a, e in ev:
+        flush.zero_()
+        a.record(stream)
+        u, _ = db.run()
+        e.record(stream)
+    torch.cuda.synchronize()
+    ms = statistics.mean(a.elapsed_time(e) for a, e in ev)
+    matched = int((u >= 0).sum().item())
+    for _ in range(2):
+        matcher.stereo_match(sb, device=local)
+    e2e_ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        matcher.stereo_match(sb, device=local)
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    clk = clocks.stop()
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle
+
+        sub = synth.stereo_batch(16, STEREO_LEFT, STEREO_CLUTTER, 7100)
+        runs, t0 = 0, time.perf_counter()
+        while True:
+            oracle.stereo_match(sub, n_threads=1)
+            runs += 1
+            if time.perf_counter() - t0 >= 3.0 or runs >= 20:
+                break
+        dtc = time.perf_counter() - t0
+        cpu = {"value": runs * 16 / dtc, "unit": "frames/s", "cores": 1, "kind": "port",
+               "sample": f"{runs} x 16 frames of the same shape, serial oracle, {dtc:.1f} s"}
+    nl, nr = int(sb.left_begin[-1]), int(sb.right_begin[-1])
+    pyr = 2 * args.frames * sb.pyr_bytes
+    h2d = pyr + sb.left_xy.nbytes + sb.left_oct.nbytes + sb.left_desc.nbytes + sb.right_xy.nbytes + \
+        sb.right_oct.nbytes + sb.right_desc.nbytes + 8 * (args.frames + 1)
+    # compulsory bytes: keypoints and descriptors once, the 11 x 21 patch
+    # bytes of the matched keypoints, the outputs
+    alg = nl * (8 + 4 + 32 + 8) + nr * (8 + 4 + 32) + matched * (11 * 11 + 11 * 21)
+    peak, peak_kind = read_peaks()
+    achieved = alg / (ms / 1e3) / 1e9
+    line = {
+        "metric": "stereo frames matched/s", "value": args.frames / (ms / 1e3), "unit": "frames/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8+i32+f32",
+        "data": "synthetic: textured pyramids, right = left shifted by the frame disparity + noise",
+        "config": {"workload": f"stereo_match_{args.frames}x{STEREO_LEFT}", "frames": args.frames,
+                   "left_keypoints": nl, "right_keypoints": nr, "kept_matches": matched, "image": "512x512x8 levels",
+                   "l2": "flushed (256 MB write) before every step"},
+        "e2e": {"value": args.frames / (statistics.mean(e2e_ms) / 1e3), "unit": "frames/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 8 * nl},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_kind": peak_kind,
+                     "note": "three kernels of one call over the compulsory bytes; latency-bound gathers"},
+        "cpu_baseline": cpu, "clocks": clk, "gpu_launches": 3 * args.steps,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_stereo_reference(args):
+    """The oracle's ComputeStereoMatch over the same frames, spread over every host thread."""
+    rank, _, _ = dist_env()
+    if rank != 0:
+        return
+    from mcvslam_gb300 import synth
+    from oracle import oracle
+
+    sb = synth.stereo_batch(args.frames, STEREO_LEFT, STEREO_CLUTTER, 7100)
+    threads = os.cpu_count() or 1
+    times = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        oracle.stereo_match(sb, n_threads=threads)
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    ms = 1e3 * statistics.mean(times)
+    value = args.frames / (ms / 1e3)
+    line = {
+        "impl": "reference", "metric": "stereo frames matched/s", "value": value, "unit": "frames/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8+i32+f32",
+        "data": "synthetic", "config": {"workload": f"stereo_match_{args.frames}x{STEREO_LEFT}"},
+        "cpu_baseline": {"value": value, "unit": "frames/s", "cores": threads, "kind": "port",
+                         "sample": "each step the whole batch, frames over OpenMP threads"},
+        "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
-    if args.workload == "project":
+    if args.workload == "stereo":
+        if args.impl == "reference":
+            run_stereo_reference(args)
+        else:
+            run_stereo(args)
+    elif args.workload == "project":
         if args.impl == "reference":
             run_project_reference(args)
         else:

@@ -335,6 +335,57 @@ int mcba_project_match(int32_t device, const mcba_projection_batch* batch, int32
 int mcba_project_match_device(const mcba_projection_batch* batch, int32_t n_kp, int32_t n_mp, int32_t* kp_bind,
                               int32_t* mp_match, int32_t* obj_count, void* stream);
 
+/* ------------------------------------------------------ stereo matching -- */
+/* Frame::ComputeStereoMatch (src/Frame.cpp:150-325) for a batch of rectified
+ * stereo frames: for each left keypoint, the right keypoints whose row band
+ * (10 x mvScaleFactor[octave] rows around their y) covers its row, within one
+ * octave and inside the disparity range [1, min(bf / b, 1000)]; k = 2 Hamming
+ * match with FilterRatio(0.70) and FilterThreshold(34); 11 x 11 SAD of
+ * centre-subtracted patches at the keypoint's pyramid level over 11 offsets;
+ * parabola sub-pixel fit; and the per-frame median filter of the best SADs.
+ * The pyramid tables are the left extractor's, as in the reference. */
+#define MCBA_MAX_LEVELS 32
+typedef struct mcba_stereo_batch {
+  int32_t n_frames;
+  int32_t n_levels;                      /* <= MCBA_MAX_LEVELS */
+  float scale[MCBA_MAX_LEVELS];          /* mvScaleFactor */
+  float inv_scale[MCBA_MAX_LEVELS];      /* mvInvScaleFactor */
+  int32_t level_rows[MCBA_MAX_LEVELS];   /* mvImagePyramid[l].rows (left and right alike) */
+  int32_t level_cols[MCBA_MAX_LEVELS];   /* mvImagePyramid[l].cols */
+  int64_t level_offset[MCBA_MAX_LEVELS]; /* byte offset of level l in one image's pyramid, rows packed */
+  int64_t pyr_bytes;                     /* bytes of one image's pyramid */
+  int32_t image_rows;                    /* left image height: rows of the row table (<= 8192) */
+  float b;                               /* baseline (minZ) */
+  float bf;                              /* baseline x fx */
+  const uint8_t* left_pyr;               /* [n_frames][pyr_bytes] */
+  const uint8_t* right_pyr;              /* [n_frames][pyr_bytes] */
+  const int32_t* left_begin;             /* [n_frames + 1], left_begin[0] = 0 */
+  const float* left_xy;                  /* [n_left][2] */
+  const int32_t* left_oct;               /* [n_left] octave */
+  const uint8_t* left_desc;              /* [n_left][32] */
+  const int32_t* right_begin;            /* [n_frames + 1], right_begin[0] = 0 */
+  const float* right_xy;                 /* [n_right][2] */
+  const int32_t* right_oct;              /* [n_right] */
+  const uint8_t* right_desc;             /* [n_right][32] */
+} mcba_stereo_batch;
+
+/* Host buffers: u_right and depth [n_left] receive the right-image u and
+ * bf / disparity of each left keypoint, -1 where there is none (Frame::u_right,
+ * Frame::depth_left).  Invalid octaves or tables, non-finite keypoints are
+ * errors.  Where the reference reads outside its arrays the result is
+ * defined: band rows outside the image are dropped, a right window starting
+ * left of column 0 gives no match, a frame without matches skips the median
+ * filter. */
+int mcba_stereo_match(int32_t device, const mcba_stereo_batch* batch, float* u_right, float* depth,
+                      double* ms_device);
+/* The same with the batch's pointers and the outputs in device memory
+ * (descriptors 16-byte aligned, positions 8-byte aligned; the tables in the
+ * struct stay host values), on `stream`; n_left = left_begin[n_frames],
+ * n_right = right_begin[n_frames].  Contents are not validated; the scratch is
+ * cached per device, so overlapping calls on one device must be serialised. */
+int mcba_stereo_match_device(const mcba_stereo_batch* batch, int32_t n_left, int32_t n_right, float* u_right,
+                             float* depth, void* stream);
+
 /* ------------------------------------------- batched local-BA windows -- */
 /* Many independent local-BA windows solved together (the windows of config
  * 4): PoseEstimation::BoundleAdjustment (include/PoseEstimation.hpp:36-119)

@@ -80,6 +80,24 @@ class ProjectionBatchDesc(ctypes.Structure):
     ]
 
 
+MAX_LEVELS = 32
+
+
+class StereoBatchDesc(ctypes.Structure):
+    """mcba_stereo_batch; pointer fields as plain addresses (host or device)."""
+    _fields_ = [
+        ("n_frames", ctypes.c_int32), ("n_levels", ctypes.c_int32),
+        ("scale", ctypes.c_float * MAX_LEVELS), ("inv_scale", ctypes.c_float * MAX_LEVELS),
+        ("level_rows", ctypes.c_int32 * MAX_LEVELS), ("level_cols", ctypes.c_int32 * MAX_LEVELS),
+        ("level_offset", ctypes.c_int64 * MAX_LEVELS), ("pyr_bytes", ctypes.c_int64),
+        ("image_rows", ctypes.c_int32), ("b", ctypes.c_float), ("bf", ctypes.c_float),
+        ("left_pyr", ctypes.c_void_p), ("right_pyr", ctypes.c_void_p),
+        ("left_begin", ctypes.c_void_p), ("left_xy", ctypes.c_void_p), ("left_oct", ctypes.c_void_p),
+        ("left_desc", ctypes.c_void_p), ("right_begin", ctypes.c_void_p), ("right_xy", ctypes.c_void_p),
+        ("right_oct", ctypes.c_void_p), ("right_desc", ctypes.c_void_p),
+    ]
+
+
 _LIB = None
 
 
@@ -140,6 +158,8 @@ def _declare(L):
                               c_double_p], ctypes.c_int),
         "mcba_project_match": ([i32, ctypes.POINTER(ProjectionBatchDesc), P, P, P, c_double_p], ctypes.c_int),
         "mcba_project_match_device": ([ctypes.POINTER(ProjectionBatchDesc), i32, i32, P, P, P, P], ctypes.c_int),
+        "mcba_stereo_match": ([i32, ctypes.POINTER(StereoBatchDesc), P, P, c_double_p], ctypes.c_int),
+        "mcba_stereo_match_device": ([ctypes.POINTER(StereoBatchDesc), i32, i32, P, P, P], ctypes.c_int),
         "mcba_robust_cost_noalloc": ([ctypes.c_int64, P, P, P, P, P, P, P, P, P, P], ctypes.c_int),
     }
     for name, (args, res) in sig.items():

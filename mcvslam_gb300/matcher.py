@@ -120,3 +120,67 @@ class DeviceProjectionBatch:
         N.check(N.lib().mcba_project_match_device(ctypes.byref(self.desc), self.nk, self.nm, self.kp_bind.data_ptr(),
                                                   self.mp_match.data_ptr(), self.count.data_ptr(), stream))
         return self.kp_bind, self.mp_match[:self.nm], self.count[:self.b.n_objects]
+
+
+_SB_FIELDS = [("left_pyr", "uint8"), ("right_pyr", "uint8"), ("left_begin", "int32"), ("left_xy", "float32"),
+              ("left_oct", "int32"), ("left_desc", "uint8"), ("right_begin", "int32"), ("right_xy", "float32"),
+              ("right_oct", "int32"), ("right_desc", "uint8")]
+
+
+def _stereo_desc(sb, arrays):
+    d = N.StereoBatchDesc()
+    d.n_frames = sb.n_frames
+    nl = int(sb.scale.shape[0])
+    if nl > N.MAX_LEVELS:
+        raise ValueError(f"at most {N.MAX_LEVELS} pyramid levels")
+    d.n_levels = nl
+    for i in range(nl):
+        d.scale[i] = float(sb.scale[i])
+        d.inv_scale[i] = float(sb.inv_scale[i])
+        d.level_rows[i] = int(sb.level_rows[i])
+        d.level_cols[i] = int(sb.level_cols[i])
+        d.level_offset[i] = int(sb.level_offset[i])
+    d.pyr_bytes = int(sb.pyr_bytes)
+    d.image_rows = int(sb.image_rows)
+    d.b = float(sb.b)
+    d.bf = float(sb.bf)
+    for name, _ in _SB_FIELDS:
+        a = arrays[name]
+        setattr(d, name, a.data_ptr() if hasattr(a, "data_ptr") else a.ctypes.data)
+    return d
+
+
+def stereo_match(sb, device: int = 0):
+    """Frame::ComputeStereoMatch over a batch of frames (host arrays of a
+    synth.StereoBatch-like object): (u_right, depth, kernel ms)."""
+    arrays = {name: np.ascontiguousarray(getattr(sb, name), dtype=dt) for name, dt in _SB_FIELDS}
+    d = _stereo_desc(sb, arrays)
+    nl = int(sb.left_begin[-1])
+    u = np.zeros(nl, np.float32)
+    z = np.zeros(nl, np.float32)
+    ms = ctypes.c_double(0.0)
+    N.check(N.lib().mcba_stereo_match(device, ctypes.byref(d), u.ctypes.data, z.ctypes.data, ctypes.byref(ms)))
+    return u, z, ms.value
+
+
+class DeviceStereoBatch:
+    """A stereo batch resident on the GPU, for repeated device-side calls."""
+
+    def __init__(self, sb, device: int = 0):
+        import torch
+
+        self.dev = torch.device("cuda", device)
+        self.t = {name: torch.from_numpy(np.ascontiguousarray(getattr(sb, name), dtype=dt)).to(self.dev)
+                  for name, dt in _SB_FIELDS}
+        self.nl, self.nr = int(sb.left_begin[-1]), int(sb.right_begin[-1])
+        self.u = torch.empty(max(self.nl, 1), dtype=torch.float32, device=self.dev)
+        self.z = torch.empty(max(self.nl, 1), dtype=torch.float32, device=self.dev)
+        self.desc = _stereo_desc(sb, self.t)
+
+    def run(self):
+        import torch
+
+        stream = torch.cuda.current_stream(self.dev).cuda_stream
+        N.check(N.lib().mcba_stereo_match_device(ctypes.byref(self.desc), self.nl, self.nr, self.u.data_ptr(),
+                                                 self.z.data_ptr(), stream))
+        return self.u[:self.nl], self.z[:self.nl]

@@ -608,3 +608,110 @@ def projection_batch(n_objects: int, n_kp: int, n_mp: int, seed: int, radius: fl
                            obj_scale=scale.astype(np.float32), ratio=0.6, max_dist=46, kp_begin=kp_begin,
                            kp_xy=kp_xy, kp_desc=kp_desc, kp_bind=kp_bind, mp_begin=mp_begin, mp_X=mp_X,
                            mp_desc=mp_desc, mp_level=mp_level, mp_id=mp_id, mp_prev_kp=mp_prev)
+
+
+@dataclasses.dataclass
+class StereoBatch:
+    """Rectified stereo frames for Frame::ComputeStereoMatch."""
+    scale: np.ndarray        # [L] float32 mvScaleFactor
+    inv_scale: np.ndarray    # [L] float32 mvInvScaleFactor
+    level_rows: np.ndarray   # [L] int32
+    level_cols: np.ndarray   # [L] int32
+    level_offset: np.ndarray  # [L] int64 byte offset of each level in one image's pyramid
+    pyr_bytes: int
+    left_pyr: np.ndarray     # [F, pyr_bytes] uint8
+    right_pyr: np.ndarray    # [F, pyr_bytes] uint8
+    image_rows: int
+    b: float
+    bf: float
+    left_begin: np.ndarray   # [F+1] int32
+    left_xy: np.ndarray      # [NL, 2] float32
+    left_oct: np.ndarray     # [NL] int32
+    left_desc: np.ndarray    # [NL, 32] uint8
+    right_begin: np.ndarray  # [F+1] int32
+    right_xy: np.ndarray     # [NR, 2] float32
+    right_oct: np.ndarray    # [NR] int32
+    right_desc: np.ndarray   # [NR, 32] uint8
+
+    @property
+    def n_frames(self):
+        return int(self.left_begin.shape[0] - 1)
+
+
+def _texture(rng, rows, cols):
+    """Smooth random uint8 texture (box-blurred noise at two scales)."""
+    a = rng.random((rows + 8, cols + 8))
+    # 5-tap box filter along each axis through cumulative sums
+    c = np.cumsum(np.pad(a, ((0, 0), (3, 2))), axis=1)
+    a = (c[:, 5:] - c[:, :-5]) / 5.0
+    c = np.cumsum(np.pad(a, ((3, 2), (0, 0))), axis=0)
+    a = (c[5:, :] - c[:-5, :]) / 5.0
+    a = (a - a.min()) / max(np.ptp(a), 1e-9)
+    return (a[4:4 + rows, 4:4 + cols] * 255).astype(np.uint8)
+
+
+def stereo_batch(n_frames: int, n_left: int, n_right_clutter: int, seed: int, size=(512, 512),
+                 fx: float = 955.40503, baseline: float = 1.0, n_levels: int = 8, match_frac: float = 0.8):
+    """Each frame: a textured left pyramid, the right pyramid shifted by the
+    frame's disparity (scaled per level) plus noise, n_left left keypoints
+    (random octave, inside the ORB border), their right counterparts for
+    match_frac of them (disparity + sub-pixel noise, perturbed descriptor,
+    octave within one level) and n_right_clutter unrelated right keypoints."""
+    rng = np.random.default_rng(seed)
+    cols0, rows0 = size
+    scale = scale_factors(n_levels)
+    inv = (np.float32(1.0) / scale).astype(np.float32)
+    lr = np.array([int(round(float(rows0) * float(s))) for s in inv], np.int32)
+    lc = np.array([int(round(float(cols0) * float(s))) for s in inv], np.int32)
+    off = np.zeros(n_levels, np.int64)
+    for i in range(1, n_levels):
+        off[i] = off[i - 1] + int(lr[i - 1]) * int(lc[i - 1])
+    pyr_bytes = int(off[-1] + int(lr[-1]) * int(lc[-1]))
+    left_pyr = np.zeros((n_frames, pyr_bytes), np.uint8)
+    right_pyr = np.zeros((n_frames, pyr_bytes), np.uint8)
+    L_xy, L_oct, L_desc, R_xy, R_oct, R_desc = [], [], [], [], [], []
+    lb, rb = [0], [0]
+    for f in range(n_frames):
+        disp = float(rng.uniform(8.0, 60.0))
+        for lev in range(n_levels):
+            rows, cols = int(lr[lev]), int(lc[lev])
+            shift = disp * float(inv[lev])
+            s_int = int(np.floor(shift))
+            tex = _texture(rng, rows, cols + s_int + 2)
+            left = tex[:, s_int:s_int + cols]
+            right = tex[:, :cols].astype(np.int16) + rng.integers(-3, 4, size=(rows, cols))
+            left_pyr[f, off[lev]:off[lev] + rows * cols] = left.reshape(-1)
+            right_pyr[f, off[lev]:off[lev] + rows * cols] = np.clip(right, 0, 255).astype(np.uint8).reshape(-1)
+        oct_ = rng.integers(0, n_levels, n_left).astype(np.int32)
+        margin = 19.0 * scale[oct_]
+        x = rng.uniform(margin + disp + 12 * scale[oct_], cols0 - margin).astype(np.float32)
+        y = rng.uniform(margin, rows0 - margin).astype(np.float32)
+        desc = rng.integers(0, 256, size=(n_left, 32), dtype=np.uint8)
+        L_xy.append(np.stack([x, y], 1))
+        L_oct.append(oct_)
+        L_desc.append(desc)
+        m = rng.random(n_left) < match_frac
+        xr = (x[m] - disp + rng.normal(0, 0.4, m.sum())).astype(np.float32)
+        yr = (y[m] + rng.normal(0, 0.4, m.sum())).astype(np.float32)
+        orr = np.clip(oct_[m] + rng.integers(-1, 2, m.sum()), 0, n_levels - 1).astype(np.int32)
+        bits = np.unpackbits(desc[m], axis=1)
+        flips = rng.random(bits.shape) < 0.04
+        dr = np.packbits(bits ^ flips.astype(np.uint8), axis=1)
+        oc = rng.integers(0, n_levels, n_right_clutter).astype(np.int32)
+        mc = 19.0 * scale[oc]
+        xc = rng.uniform(mc, cols0 - mc).astype(np.float32)
+        yc = rng.uniform(mc, rows0 - mc).astype(np.float32)
+        dc = rng.integers(0, 256, size=(n_right_clutter, 32), dtype=np.uint8)
+        perm = rng.permutation(m.sum() + n_right_clutter)
+        R_xy.append(np.concatenate([np.stack([xr, yr], 1), np.stack([xc, yc], 1)])[perm])
+        R_oct.append(np.concatenate([orr, oc])[perm])
+        R_desc.append(np.concatenate([dr, dc])[perm])
+        lb.append(lb[-1] + n_left)
+        rb.append(rb[-1] + int(m.sum()) + n_right_clutter)
+    return StereoBatch(scale=scale, inv_scale=inv, level_rows=lr, level_cols=lc, level_offset=off,
+                       pyr_bytes=pyr_bytes, left_pyr=left_pyr, right_pyr=right_pyr, image_rows=rows0,
+                       b=float(baseline), bf=float(np.float32(fx * baseline)), left_begin=np.array(lb, np.int32),
+                       left_xy=np.concatenate(L_xy).astype(np.float32), left_oct=np.concatenate(L_oct),
+                       left_desc=np.concatenate(L_desc), right_begin=np.array(rb, np.int32),
+                       right_xy=np.concatenate(R_xy).astype(np.float32), right_oct=np.concatenate(R_oct),
+                       right_desc=np.concatenate(R_desc))

@@ -11,7 +11,10 @@
 
 #include <stdint.h>
 
+#include <algorithm>
+#include <climits>
 #include <cmath>
+#include <utility>
 #include <unordered_map>
 #include <vector>
 
@@ -186,6 +189,162 @@ void orc_project_match(int32_t n_threads, int32_t n_objects, const float* obj_Rt
       ++cnt;
     }
     obj_count[o] = cnt;
+  }
+}
+
+// Frame::ComputeStereoMatch (src/Frame.cpp:150-325) over a batch of stereo
+// frames, restated literally: the row table of right keypoints (band of
+// 10 * mvScaleFactor[octave] rows around each), per left keypoint the
+// candidates of its row within one octave and the disparity range, KnnMatch
+// k = 2 with FilterRatio(0.70) and FilterThreshold(int(46 * 0.75) = 34), the
+// 11 x 11 SAD of centre-subtracted patches over 11 offsets at the keypoint's
+// pyramid level, parabola sub-pixel fit, disparity test, and the median
+// filter of the best SAD distances.  Pyramids: per frame one byte buffer of
+// pyr_bytes, level l row-major at level_offset[l], level_rows[l] x
+// level_cols[l].  Outputs u_right and depth per left keypoint (-1: none).
+// Where the reference reads outside its arrays, this restatement defines the
+// result: rows of the band outside [0, image_rows) are dropped, a left
+// keypoint whose row is outside the table has no candidates, a right window
+// starting left of column 0 skips the keypoint (OpenCV would throw), and a
+// frame without matches skips the median filter (the reference indexes an
+// empty vector).
+void orc_stereo_match(int32_t n_threads, int32_t n_frames, int32_t n_levels, const float* scale,
+                      const float* inv_scale, const int32_t* level_rows, const int32_t* level_cols,
+                      const int64_t* level_offset, int64_t pyr_bytes, const uint8_t* left_pyr,
+                      const uint8_t* right_pyr, int32_t image_rows, float b, float bf, const int32_t* left_begin,
+                      const float* left_xy, const int32_t* left_oct, const uint8_t* left_desc,
+                      const int32_t* right_begin, const float* right_xy, const int32_t* right_oct,
+                      const uint8_t* right_desc, float* u_right, float* depth) {
+  (void)n_levels;
+#pragma omp parallel for num_threads(n_threads > 0 ? n_threads : 1) schedule(dynamic, 1) if (n_threads > 1)
+  for (int32_t f = 0; f < n_frames; ++f) {
+    const int32_t l0 = left_begin[f], nl = left_begin[f + 1] - l0;
+    const int32_t r0 = right_begin[f], nr = right_begin[f + 1] - r0;
+    const uint8_t* LP = left_pyr + (size_t)f * pyr_bytes;
+    const uint8_t* RP = right_pyr + (size_t)f * pyr_bytes;
+    float* ur = u_right + l0;
+    float* dp = depth + l0;
+    for (int i = 0; i < nl; ++i) {
+      ur[i] = -1.0f;
+      dp[i] = -1.0f;
+    }
+    const int nRows = image_rows;
+    std::vector<std::vector<int>> rows((size_t)nRows);
+    for (int iR = 0; iR < nr; ++iR) {
+      const float kpY = right_xy[2 * (size_t)(r0 + iR) + 1];
+      const float r = 10.f * scale[right_oct[r0 + iR]];
+      const int maxr = (int)std::ceil(kpY + r);
+      const int minr = (int)std::floor(kpY - r);
+      for (int yi = std::max(minr, 0); yi <= std::min(maxr, nRows - 1); ++yi) rows[yi].push_back(iR);
+    }
+    const float minZ = b;
+    const float minD = 1;
+    const float maxD = std::min(bf / minZ, float(1000.0));
+    std::vector<std::pair<int, int>> vDistIdx;
+    for (int iL = 0; iL < nl; ++iL) {
+      const int levelL = left_oct[l0 + iL];
+      const float vL = left_xy[2 * (size_t)(l0 + iL) + 1];
+      const float uL = left_xy[2 * (size_t)(l0 + iL)];
+      if (!(vL >= 0) || (size_t)vL >= (size_t)nRows) continue;
+      const std::vector<int>& cands = rows[(size_t)vL];
+      if (cands.empty()) continue;
+      const float minU = uL - maxD;
+      const float maxU = uL - minD;
+      if (maxU < 0) continue;
+      std::vector<int> cand;
+      for (int iR : cands) {
+        const int o = right_oct[r0 + iR];
+        if (o < levelL - 1 || o > levelL + 1) continue;
+        const float uR = right_xy[2 * (size_t)(r0 + iR)];
+        if (uR >= minU && uR <= maxU) cand.push_back(iR);
+      }
+      if (cand.empty()) continue;
+      const uint32_t* q = reinterpret_cast<const uint32_t*>(left_desc + 32 * (size_t)(l0 + iL));
+      unsigned d[2] = {999, 999};
+      unsigned di[2] = {0, 0};
+      for (size_t j = 0; j < cand.size(); ++j) {
+        const unsigned dj = hamming(q, reinterpret_cast<const uint32_t*>(right_desc + 32 * (size_t)(r0 + cand[j])));
+        if (dj < d[0]) {
+          d[1] = d[0];
+          di[1] = di[0];
+          d[0] = dj;
+          di[0] = (unsigned)j;
+        } else if (dj < d[1]) {
+          d[1] = dj;
+          di[1] = (unsigned)j;
+        }
+      }
+      if (!((float)d[0] / (float)d[1] <= 0.70f)) continue;
+      if ((float)d[0] > (float)(int)(46 * 0.75)) continue;
+      const float uR0 = right_xy[2 * (size_t)(r0 + cand[di[0]])];
+      const float scaleFactor = inv_scale[levelL];
+      const float scaleduL = std::round(uL * scaleFactor);
+      const float scaledvL = std::round(vL * scaleFactor);
+      const float scaleduR0 = std::round(uR0 * scaleFactor);
+      const int w = 5;
+      const int rowsL = level_rows[levelL], colsL = level_cols[levelL];
+      if (scaledvL - w < 0 || scaledvL + w + 1 >= rowsL || scaleduL - w < 0 || scaleduL + w + 1 >= colsL) continue;
+      const uint8_t* imL = LP + level_offset[levelL];
+      const uint8_t* imR = RP + level_offset[levelL];
+      const int yv = (int)scaledvL, xl = (int)scaleduL, xr = (int)scaleduR0;
+      short IL[11][11];
+      for (int rr = 0; rr < 11; ++rr)
+        for (int cc = 0; cc < 11; ++cc) IL[rr][cc] = (short)imL[(size_t)(yv - w + rr) * colsL + (xl - w + cc)];
+      const short cL = IL[w][w];
+      for (int rr = 0; rr < 11; ++rr)
+        for (int cc = 0; cc < 11; ++cc) IL[rr][cc] = (short)(IL[rr][cc] - cL);
+      int bestDist = INT_MAX;
+      int bestincR = 0;
+      const int L = 5;
+      float vDists[2 * L + 1];
+      const float iniu = scaleduR0 + L - w;
+      const float endu = scaleduR0 + L + w + 1;
+      if (iniu < 0 || endu >= colsL) continue;
+      if (xr - L - w < 0) continue;  // the reference's colRange would throw here
+      for (int incR = -L; incR <= +L; ++incR) {
+        const int x0 = xr + incR - w;
+        const short cR = (short)imR[(size_t)yv * colsL + (xr + incR)];
+        double acc = 0.0;
+        for (int rr = 0; rr < 11; ++rr)
+          for (int cc = 0; cc < 11; ++cc) {
+            const short vR = (short)((short)imR[(size_t)(yv - w + rr) * colsL + (x0 + cc)] - cR);
+            acc += std::abs((int)IL[rr][cc] - (int)vR);
+          }
+        const float dist = (float)acc;
+        if (dist < bestDist) {
+          bestDist = (int)dist;
+          bestincR = incR;
+        }
+        vDists[L + incR] = dist;
+      }
+      if (bestincR == -L || bestincR == L) continue;
+      const float dist1 = vDists[L + bestincR - 1];
+      const float dist2 = vDists[L + bestincR];
+      const float dist3 = vDists[L + bestincR + 1];
+      const float deltaR = (dist1 - dist3) / (2.0f * (dist1 + dist3 - 2.0f * dist2));
+      if (deltaR < -1 || deltaR > 1) continue;
+      const float bestuR = scale[levelL] * ((float)scaleduR0 + (float)bestincR + deltaR);
+      const float disparity = (uL - bestuR);
+      if (disparity >= minD && disparity < maxD) {
+        dp[iL] = bf / disparity;
+        ur[iL] = bestuR;
+        vDistIdx.push_back(std::pair<int, int>(bestDist, iL));
+      }
+    }
+    if (vDistIdx.empty()) continue;
+    std::sort(vDistIdx.begin(), vDistIdx.end());
+    const float median = vDistIdx[vDistIdx.size() * 1.0 / 2].first;
+    const float th_max_dist = 1.6f * median;
+    const float th_min_dist = 0.4 * median;
+    int l = 0, r = (int)vDistIdx.size() - 1;
+    for (; r >= 0 && vDistIdx[r].first > th_max_dist; r--) {
+      ur[vDistIdx[r].second] = -1;
+      dp[vDistIdx[r].second] = -1;
+    }
+    for (; l < r && vDistIdx[l].first < th_min_dist; l++) {
+      ur[vDistIdx[l].second] = -1;
+      dp[vDistIdx[l].second] = -1;
+    }
   }
 }
 

@@ -287,3 +287,33 @@ def project_match(b, n_threads: int = 1):
                         p[5], p[6], p[7], p[8], p[9], p[10], p[11], p[12], _ptr(kp_bind, c_i), _ptr(mp_match, c_i),
                         _ptr(obj_count, c_i))
     return kp_bind, mp_match, obj_count
+
+
+def stereo_match(sb, n_threads: int = 1):
+    """Frame::ComputeStereoMatch over a synth.StereoBatch: (u_right, depth) per left keypoint."""
+    L = lib(n_threads > 1)
+    c_f, c_i, c_u8 = c_float_p, c_i32_p, c_u8_p
+    c_i64 = ctypes.POINTER(ctypes.c_int64)
+    if not hasattr(L, "_sm_sig"):
+        i32 = ctypes.c_int32
+        L.orc_stereo_match.argtypes = [i32, i32, i32, c_f, c_f, c_i, c_i, c_i64, ctypes.c_int64, c_u8, c_u8, i32,
+                                       ctypes.c_float, ctypes.c_float, c_i, c_f, c_i, c_u8, c_i, c_f, c_i, c_u8,
+                                       c_f, c_f]
+        L.orc_stereo_match.restype = None
+        L._sm_sig = True
+    a = lambda x, dt: np.ascontiguousarray(x, dt)  # noqa: E731
+    k = dict(scale=a(sb.scale, np.float32), inv=a(sb.inv_scale, np.float32), lr=a(sb.level_rows, np.int32),
+             lc=a(sb.level_cols, np.int32), off=a(sb.level_offset, np.int64), lp=a(sb.left_pyr, np.uint8),
+             rp=a(sb.right_pyr, np.uint8), lb=a(sb.left_begin, np.int32), lxy=a(sb.left_xy, np.float32),
+             lo=a(sb.left_oct, np.int32), ld=a(sb.left_desc, np.uint8), rb=a(sb.right_begin, np.int32),
+             rxy=a(sb.right_xy, np.float32), ro=a(sb.right_oct, np.int32), rd=a(sb.right_desc, np.uint8))
+    nl = int(sb.left_begin[-1])
+    u = np.zeros(nl, np.float32)
+    d = np.zeros(nl, np.float32)
+    L.orc_stereo_match(n_threads, sb.n_frames, int(sb.scale.shape[0]), _ptr(k["scale"], c_f), _ptr(k["inv"], c_f),
+                       _ptr(k["lr"], c_i), _ptr(k["lc"], c_i), _ptr(k["off"], c_i64), int(sb.pyr_bytes),
+                       _ptr(k["lp"], c_u8), _ptr(k["rp"], c_u8), int(sb.image_rows), float(sb.b), float(sb.bf),
+                       _ptr(k["lb"], c_i), _ptr(k["lxy"], c_f), _ptr(k["lo"], c_i), _ptr(k["ld"], c_u8),
+                       _ptr(k["rb"], c_i), _ptr(k["rxy"], c_f), _ptr(k["ro"], c_i), _ptr(k["rd"], c_u8),
+                       _ptr(u, c_f), _ptr(d, c_f))
+    return u, d
