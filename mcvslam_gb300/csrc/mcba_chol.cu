@@ -8,28 +8,33 @@
 // squares of the Cholesky diagonal, so "d_j <= 0" is the same failure test,
 // and the solution is the same up to round-off.
 //
-// Cost model on GB300: an FP64 warp instruction occupies its SM
-// sub-partition for ~64 cycles whatever the number of active lanes, an SM
-// retires ~2 FP64 FMA per clock, and a distributed-shared-memory load waits
-// ~2k cycles.  So the design (a) spreads the bulk FP64 work over the CTAs of
-// one non-portable cluster (16), (b) keeps the pivot chain at five FP64
-// instructions per pivot on four warps, one per sub-partition, (c) keeps
-// the lanes of the bulk FP64 instructions busy and (d) pushes data to the
-// CTAs that need it (remote stores, visible at the next cluster barrier)
-// instead of pulling it:
-//   * the lower triangle is cut into 16x16 tiles (tile t = i(i+1)/2 + j, the
-//     right-hand side b is an extra block row); tile t lives in the shared
-//     memory of CTA t mod C;
-//   * step k: the owner of diagonal tile k has factored it and pushed it to
-//     every CTA; the owners of the panel tiles (i,k) solve them against it,
-//     one warp per two rows with shuffles, and push W = L D and L to the CTAs
-//     whose share of the trailing update reads them; the trailing tiles are
-//     dealt in contiguous ranges and updated in place at their owners;
-//   * look-ahead: the owner of diagonal tile k+1 updates it first, factors it
-//     and pushes it while the other CTAs finish the trailing update;
-//   * the right-hand-side row leaves y = D^-1 L^-1 b; CTA 0 then solves
-//     L^T x = y block row by block row, streaming row J-1 of L in while it
-//     works on row J.
+// Cost model on GB300 (measured): a dependent FP64 FMA takes 64 cycles and an
+// SM retires ~1.6 FP64 FMA per clock; a cluster barrier costs ~400 cycles;
+// distributed-shared-memory stores move only ~13 B per clock per SM, while
+// the 129 MB L2 serves an SM several times faster.  So the bulk FP64 work is
+// spread over the CTAs of one 16-CTA cluster, the barriers are the cluster's,
+// and the tiles themselves live in an L2-resident workspace (same shape as
+// S; S is only read), so any CTA can update any tile:
+//   * the lower triangle is cut into 16x16 tiles, the right-hand side b is an
+//     extra block row;
+//   * step k, panel: the CTA D(k+1) chosen for diagonal tile (k+1, k+1)
+//     solves panel tile (k+1, k) itself (keeping W and L of it in shared
+//     memory) and prefetches tile (k+1, k+1); the other panel tiles (i, k),
+//     k+1 < i <= nblk, are spread over the other CTAs.  Each is solved
+//     against L_kk and 1/d_k, and W_ik = L_ik D_k is written over it (lower
+//     tile (i, k)) and L_ik into the upper tile (k, i); the right-hand-side
+//     tile leaves W in row ld and y_k = D^-1 L^-1 b in row ld + 2;
+//   * step k, update: D(k+1) applies step k to its diagonal tile, factors it
+//     (the pivot chain alone on one warp) and writes L, d and 1/d (row
+//     ld + 1); the other trailing tiles are dealt in contiguous ranges, D
+//     taking a reduced share after its factorisation.  Each CTA stages the
+//     panel rows and columns its range needs in shared memory and keeps eight
+//     tiles (and eight L2 loads per thread) in flight;
+//   * CTA 0 then solves L^T x = y block row by block row, staging the next
+//     block row while warp 0 works on the current one.
+// Failure (a pivot <= 0) clears *solve_ok in global memory; CTA 0 reads it
+// after the last barrier and then leaves x untouched.  No CTA reads another
+// CTA's shared memory, so CTAs may leave as soon as they are done.
 
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
@@ -39,16 +44,17 @@
 
 #include "mcba_chol.h"
 
-namespace cg = cooperative_groups;
-
 namespace mcba {
 namespace {
+
+namespace cg = cooperative_groups;
 
 constexpr int kB = 16;  // tile edge
 constexpr int kThreads = 256;
 constexpr int kTile = kB * kB;
 constexpr int kPad = kB + 1;  // row stride of staged L tiles (conflict-free column reads)
 constexpr int kPadTile = kB * kPad;
+constexpr int kMaxBlk = 24;  // block rows handled by the cluster solve (n <= 384)
 
 // Reciprocal of a pivot: rcp.approx.ftz.f64 (relative error ~1e-6), then one
 // cubic Newton-Raphson step y (1 + e + e^2), e = 1 - d y, which leaves an
@@ -77,35 +83,35 @@ __host__ __device__ inline int tri_row(int t) {
   return a;
 }
 
-constexpr int kMaxBlk = 24;  // block rows handled by the cluster solve (n <= 384)
-
 struct Geo {
-  int C, nblk, ld, n, nslots;
-  __host__ __device__ int nT0() const { return nblk * (nblk + 1) / 2; }
-  __host__ __device__ int ntiles() const { return nT0() + nblk; }
-  __host__ __device__ int tile(int i, int j) const { return i < nblk ? i * (i + 1) / 2 + j : nT0() + j; }
-  __host__ __device__ int owner(int i, int j) const { return tile(i, j) % C; }
-  __host__ __device__ int slot(int i, int j) const { return tile(i, j) / C; }
+  int C, nblk, ld, n;
   // shared-memory layout (doubles), identical in every CTA
-  __host__ __device__ size_t o_w() const { return (size_t)nslots * kTile; }          // W = L D of panel tiles
-  __host__ __device__ size_t o_rd() const { return 2 * (size_t)nslots * kTile; }     // 1/d per diagonal slot
-  __host__ __device__ size_t o_stw() const { return o_rd() + (size_t)nslots * kB; }  // pushed W tiles [nblk+1]
-  __host__ __device__ size_t o_stl() const { return o_stw() + (size_t)(nblk + 1) * kTile; }  // pushed L [nblk]
-  __host__ __device__ size_t o_lkk() const { return o_stl() + (size_t)nblk * kPadTile; }     // pushed L_kk, 1/d_k
-  __host__ __device__ size_t o_t() const { return o_lkk() + kPadTile + kB; }          // backward-solve t [16 nblk]
-  __host__ __device__ size_t o_flag() const { return o_t() + (size_t)kB * nblk; }
-  __host__ __device__ size_t total() const { return o_flag() + 2; }
+  __host__ __device__ size_t o_stw() const { return 0; }                                      // W rows [nblk+1]
+  __host__ __device__ size_t o_stl() const { return (size_t)(nblk + 1) * kTile; }             // L [nblk]
+  __host__ __device__ size_t o_lkk() const { return o_stl() + (size_t)nblk * kPadTile; }     // L_kk, 1/d_k
+  __host__ __device__ size_t o_diag() const { return o_lkk() + kPadTile + kB; }  // D's tile, 1/d, squares
+  __host__ __device__ size_t o_t() const { return o_diag() + kTile + 2 * kB; }               // backward-solve t
+  __host__ __device__ size_t total() const { return o_t() + (size_t)kB * nblk; }
+  // backward solve: two block rows of L, over the (then idle) staging areas
+  __host__ __device__ size_t o_buf() const { return o_stw(); }
+  // the CTA that factors diagonal tile k
+  __host__ __device__ int diag_cta(int k) const { return (k * 7 + 3) % C; }
 };
 
-__device__ __forceinline__ void tile_ij(const Geo& g, int t, int& i, int& j) {
-  const int nT0 = g.nT0();
-  if (t >= nT0) {
-    i = g.nblk;
-    j = t - nT0;
-    return;
-  }
-  i = tri_row(t);
-  j = t - i * (i + 1) / 2;
+// Workspace (row stride ld, ld + 32 rows): the lower triangle of S, updated in
+// place; W_ik over the lower tile (i, k) once step k is done, L_ik in the
+// upper tile (k, i) stored as its own 16x16 array, L_kk and d in the diagonal
+// tile; right-hand side: b then W in row ld, 1/d in row ld + 1, y in row
+// ld + 2.
+__device__ __forceinline__ double* ws_lower(double* ws, int ld, int i, int k) {
+  return ws + (size_t)(kB * i) * ld + kB * k;
+}
+__device__ __forceinline__ double* ws_upper(double* ws, int ld, int j, int k) {
+  return ws + (size_t)(kB * k) * ld + kB * j;
+}
+// element (rr, cc) of tile (i, j) of the updated matrix; block row nblk is b
+__device__ __forceinline__ double* ws_tile(double* ws, int ld, int nblk, int i, int j, int rr, int cc) {
+  return (i < nblk) ? ws_lower(ws, ld, i, j) + (size_t)rr * ld + cc : ws + (size_t)ld * ld + kB * j + cc;
 }
 
 // Trailing-update list of step k: tiles (i,j), k < j <= i < nblk, row by
@@ -126,9 +132,9 @@ __device__ __forceinline__ void trail_ij(const Geo& g, int k, int L, int& i, int
 
 // Entries [lo, hi) of the step-k list updated by CTA x, and the panel tiles
 // it needs: W of block rows [rmin, rmax], L of block columns [cmin, cmax].
-// The owner D of tile (k+1, k+1) takes entry 0 and factors that tile (about
-// four tiles of work), then a reduced share; the other CTAs split the rest
-// in contiguous ranges.
+// D takes entry 0 (the next diagonal tile, which it then factors: about four
+// tiles of work) and then a reduced share; the other CTAs split the rest in
+// contiguous ranges.
 struct Need {
   int lo, hi, rmin, rmax, cmin, cmax;
 };
@@ -136,7 +142,7 @@ __device__ __forceinline__ Need trail_need(const Geo& g, int k, int x) {
   const int C = g.C, nblk = g.nblk;
   const int nrem = nblk - 1 - k;
   const int m = nrem * (nrem + 1) / 2 + nrem;
-  const int D = g.owner(k + 1, k + 1);
+  const int D = g.diag_cta(k + 1);
   const int q = (m + 4 + C - 1) / C;
   const int qD = min(max(0, q - 5), m - 1);
   const int rest = m - 1 - qD;
@@ -149,159 +155,226 @@ __device__ __forceinline__ Need trail_need(const Geo& g, int k, int x) {
   nd.rmax = -1;
   nd.cmin = nblk;
   nd.cmax = -1;
-  if (x == D) nd.rmin = nd.rmax = nd.cmin = nd.cmax = k + 1;
   if (nd.hi > nd.lo) {
     int i0, j0, i1, j1;
     trail_ij(g, k, nd.lo, i0, j0);
     trail_ij(g, k, nd.hi - 1, i1, j1);
-    nd.rmin = min(nd.rmin, i0);
-    nd.rmax = max(nd.rmax, i1);
+    nd.rmin = i0;
+    nd.rmax = i1;
     if (i0 == i1) {
-      nd.cmin = min(nd.cmin, j0);
-      nd.cmax = max(nd.cmax, j1);
+      nd.cmin = j0;
+      nd.cmax = j1;
     } else {
-      nd.cmin = min(nd.cmin, k + 1);
-      nd.cmax = max(nd.cmax, (i1 == nblk) ? nblk - 1 : i1);
+      nd.cmin = k + 1;
+      nd.cmax = (i1 == nblk) ? nblk - 1 : i1;
     }
   }
   return nd;
 }
 
-// L D L^T of one 16x16 diagonal tile in place, by threads 0-127: strict
-// lower part <- L, diagonal <- d, rd <- 1/d.  Entry (i, m), 1 <= m <= i,
-// is updated by thread tid = i(i-1)/2 + m - 1 (120 threads, one FP64 FMA per
-// pivot each); the pivot test runs once at the end on the diagonal.
-__device__ void diag_ldlt(double* T, double* rd, int* fail) {
-  const int tid = threadIdx.x;
-  const bool has = tid < 120;
-  const int a = tri_row(has ? tid : 0);
-  const int ui = a + 1, um = (has ? tid : 0) - a * (a + 1) / 2 + 1;
-  double* Tu = T + ui * kB + um;
-  for (int j = 0; j < kB; ++j) {
-    bar_named(1, 128);
-    const double d = T[j * kB + j];
-    const bool act = has && um > j;
-    double prod = 0.0;
-    if (act) prod = T[ui * kB + j] * T[um * kB + j];
-    const double r = recip_pivot(d);
-    if (tid == 0) rd[j] = r;
-    if (act) *Tu = fma(-prod, r, *Tu);
-  }
-  bar_named(1, 128);
-  if (tid < kB && !(T[tid * kB + tid] > 0.0)) *fail = 1;
-  if (has) T[ui * kB + (um - 1)] *= rd[um - 1];
-}
-
-// D pushes the factorised diagonal tile (strict lower L) and 1/d into the
-// staging area of every CTA of the cluster.
-__device__ __forceinline__ void push_lkk(cg::cluster_group& cl, double* sm, const Geo& g, int k) {
-  const int tid = threadIdx.x;
-  const int s = g.slot(k, k);
-  const double v = sm[(size_t)s * kTile + tid];
-  const double rv = (tid < kB) ? sm[g.o_rd() + (size_t)s * kB + tid] : 0.0;
-  for (int x = 0; x < g.C; ++x) {
-    double* dst = cl.map_shared_rank(sm + g.o_lkk(), x);
-    dst[(tid >> 4) * kPad + (tid & 15)] = v;
-    if (tid < kB) dst[kPadTile + tid] = rv;
+// Stage W_{i,k} for rows [r0, r1] and L_{j,k} for columns [c0, c1] from the
+// workspace, eight tiles per round so that each thread has eight L2 loads in
+// flight.
+__device__ void stage_panel(const Geo& g, double* ws, int k, int r0, int r1, int c0, int c1, double* stW,
+                            double* stL) {
+  const int tid = threadIdx.x, rr = tid >> 4, cc = tid & 15;
+  const int nblk = g.nblk, ld = g.ld;
+  const int nr = max(0, r1 - r0 + 1), nc = max(0, c1 - c0 + 1), nt = nr + nc;
+  for (int base = 0; base < nt; base += 8) {
+    double v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      v[u] = 0.0;
+      const int e = base + u;
+      if (e < nr) {
+        const int i = r0 + e;
+        if (i < nblk || rr == 0) v[u] = __ldcg(ws_tile(ws, ld, nblk, i, k, rr, cc));
+      } else if (e < nt) {
+        v[u] = __ldcg(ws_upper(ws, ld, c0 + e - nr, k) + (size_t)rr * ld + cc);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = base + u;
+      if (e < nr)
+        stW[(size_t)(r0 + e) * kTile + tid] = v[u];
+      else if (e < nt)
+        stL[(size_t)(c0 + e - nr) * kPadTile + rr * kPad + cc] = v[u];
+    }
   }
 }
 
-__global__ void __launch_bounds__(kThreads) k_ldlt_cluster(const double* __restrict__ S, int ld, int n, double* x,
-                                                           int* solve_ok, Geo g) {
+// L D L^T of one 16x16 diagonal tile in place: strict lower part <- L,
+// diagonal <- d, rd <- 1/d.  The pivot chain runs alone on warp 0 (its own
+// sub-partition, so no other FP64 work queues in front of it): from r_j it
+// forms d_{j+1} = a_{j+1,j+1} - a_{j+1,j}^2 r_j itself and takes its
+// reciprocal, while warps 1-3 and 5-7 apply pivot j to the other entries
+// (entry (i, m), 1 <= m <= i, on update thread u = i(i-1)/2 + m - 1; the
+// diagonal entry skips the pivot that warp 0 applies, and entry (i, i-1)
+// leaves its square in sq[i] once final).  One named barrier per pivot;
+// warp 4 takes no part.  The arithmetic is the plain right-looking LDL^T.
+__device__ void diag_ldlt(double* T, double* rd, double* sq, int* solve_ok) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  constexpr int kPart = 224;  // warps 0-3 and 5-7
+  if (warp == 0) {
+    double r = recip_pivot(T[0]);
+    if (lane == 0) rd[0] = r;
+    for (int j = 0; j < kB; ++j) {
+      bar_named(1, kPart);  // pivot j-1 applied everywhere, r_j published
+      if (j + 1 < kB) {
+        const double s = (j == 0) ? T[kB] * T[kB] : sq[j + 1];
+        const double d = fma(-s, r, T[(j + 1) * kB + j + 1]);
+        if (lane == 0) T[(j + 1) * kB + j + 1] = d;
+        r = recip_pivot(d);
+        if (lane == 0) rd[j + 1] = r;
+      }
+    }
+    bar_named(1, kPart);
+  } else {
+    const int u = (warp < 4) ? (warp - 1) * 32 + lane : (warp - 2) * 32 + lane;
+    const bool has = u < 120;
+    const int a = tri_row(has ? u : 0);
+    const int ui = a + 1, um = (has ? u : 0) - a * (a + 1) / 2 + 1;
+    double* Tu = T + ui * kB + um;
+    for (int j = 0; j < kB; ++j) {
+      bar_named(1, kPart);
+      if (has && um > j && !(ui == um && um == j + 1)) {
+        const double prod = T[ui * kB + j] * T[um * kB + j];
+        const double v = fma(-prod, rd[j], *Tu);
+        *Tu = v;
+        if (um == ui - 1 && j == um - 1) sq[ui] = v * v;
+      }
+    }
+    bar_named(1, kPart);
+    if (has) T[ui * kB + (um - 1)] *= rd[um - 1];
+  }
+  if (tid < kB && !(T[tid * kB + tid] > 0.0)) *solve_ok = 0;
+}
+
+// Factor the diagonal tile held in shared memory T and publish L, d, 1/d.
+__device__ void factor_publish(const Geo& g, double* ws, double* T, int k, int* solve_ok) {
+  const int tid = threadIdx.x, rr = tid >> 4, cc = tid & 15;
+  double* rd = T + kTile;
+  double* sq = rd + kB;
+  if ((tid >> 5) != 4) diag_ldlt(T, rd, sq, solve_ok);
+  __syncthreads();
+  ws_lower(ws, g.ld, k, k)[(size_t)rr * g.ld + cc] = T[tid];
+  if (tid < kB) ws[(size_t)(g.ld + 1) * g.ld + kB * k + tid] = rd[tid];
+}
+
+__global__ void __launch_bounds__(kThreads) k_ldlt_cluster(const double* __restrict__ S, double* ws, int ld, int n,
+                                                           double* x, int* solve_ok, Geo g) {
   extern __shared__ double sm[];
   cg::cluster_group cl = cg::this_cluster();
   const int r = (int)cl.block_rank();
   const int C = g.C, nblk = g.nblk;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  int* flag = reinterpret_cast<int*>(sm + g.o_flag());
-  int* flag0 = cl.map_shared_rank(flag, 0);
-  __shared__ Need s_need[16];
+  const int rr = tid >> 4, cc = tid & 15;
   __shared__ double s_x[kB];
-
-  // owned tiles from the lower triangle of S (rows n..ld-1 of S are the
-  // identity); right-hand-side tiles keep b in row 0
-  for (int t = r; t < g.ntiles(); t += C) {
-    int i, j;
-    tile_ij(g, t, i, j);
-    const int rr = tid >> 4, cc = tid & 15;
-    double v;
-    if (i < nblk)
-      v = S[(size_t)(kB * i + rr) * ld + kB * j + cc];
-    else
-      v = (rr == 0) ? S[(size_t)ld * ld + kB * j + cc] : 0.0;
-    sm[(size_t)(t / C) * kTile + tid] = v;
-  }
-  if (tid == 0) flag[0] = 0;
-  cl.sync();
-  if (g.owner(0, 0) == r) {
-    if (tid < 128) diag_ldlt(sm + (size_t)g.slot(0, 0) * kTile, sm + g.o_rd() + (size_t)g.slot(0, 0) * kB, flag0);
-    __syncthreads();
-    push_lkk(cl, sm, g, 0);
-  }
-  cl.sync();
-
+  __shared__ int s_mine[kMaxBlk + 2];  // panel tiles of this CTA, count last
   double* stW = sm + g.o_stw();
   double* stL = sm + g.o_stl();
-  for (int k = 0; k < nblk; ++k) {
-    // ---- panel: tiles (i, k), k < i <= nblk, solved by their owners against
-    //      the pushed diagonal block, then pushed to the CTAs of step k's
-    //      trailing update that need them
-    {
-      int mine = 0;
-      for (int i = k + 1; i <= nblk; ++i) mine += (g.owner(i, k) == r);
-      if (mine) {
-        if (k + 1 < nblk && tid < C) s_need[tid] = trail_need(g, k, tid);
-        const double* Lkk = sm + g.o_lkk();
-        // work items (panel tile, row pair); warp w takes items w, w + 8, ...
-        int item = 0;
-        for (int i = k + 1; i <= nblk; ++i) {
-          if (g.owner(i, k) != r) continue;
-          const int npair = (i < nblk) ? kB / 2 : 1;
-          for (int p = 0; p < npair; ++p, ++item) {
-            if ((item & 7) != warp) continue;
-            const int s = g.slot(i, k);
-            double* T = sm + (size_t)s * kTile;
-            double* W = sm + g.o_w() + (size_t)s * kTile;
-            const int row = 2 * p + (lane >> 4), c = lane & 15;
-            double a = T[row * kB + c];
+  double* Lkk = sm + g.o_lkk();
+  double* Td = sm + g.o_diag();
+
+  // copy the lower triangle of S (rows n..ld-1 are the identity) and b into
+  // the workspace, tiles dealt round robin; tile (0, 0) goes straight to
+  // D(0), which factors it and publishes the factor in its place
+  const int nT0 = nblk * (nblk + 1) / 2;
+  for (int t0 = r; t0 < nT0 + nblk; t0 += 8 * C) {
+    // eight tiles per round: eight loads in flight per thread
+    double v[8];
 #pragma unroll
-            for (int q = 0; q < kB - 1; ++q) {
-              const double wq = __shfl_sync(0xffffffffu, a, (lane & 16) | q);
-              if (c > q) a = fma(-wq, Lkk[c * kPad + q], a);
-            }
-            W[row * kB + c] = a;
-            T[row * kB + c] = a * Lkk[kPadTile + c];
-          }
+    for (int u = 0; u < 8; ++u) {
+      const int t = t0 + u * C;
+      v[u] = 0.0;
+      if (t < nT0) {
+        const int i = tri_row(t), j = t - i * (i + 1) / 2;
+        v[u] = S[(size_t)(kB * i + rr) * ld + kB * j + cc];
+      } else if (t < nT0 + nblk && rr == 0) {
+        v[u] = S[(size_t)ld * ld + kB * (t - nT0) + cc];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int t = t0 + u * C;
+      if (t == 0 || t >= nT0 + nblk) continue;
+      if (t < nT0) {
+        const int i = tri_row(t), j = t - i * (i + 1) / 2;
+        ws_lower(ws, ld, i, j)[(size_t)rr * ld + cc] = v[u];
+      } else if (rr == 0) {
+        ws[(size_t)ld * ld + kB * (t - nT0) + cc] = v[u];
+      }
+    }
+  }
+  if (g.diag_cta(0) == r) {
+    Td[tid] = S[(size_t)rr * ld + cc];
+    __syncthreads();
+    factor_publish(g, ws, Td, 0, solve_ok);
+  }
+  cl.sync();
+
+  for (int k = 0; k < nblk; ++k) {
+    // ---- panel.  Tile (k+1, k) goes to D(k+1), which keeps W and L of it in
+    //      shared memory for its diagonal update and prefetches tile
+    //      (k+1, k+1); the other panel tiles are spread over the other CTAs
+    const int Dn = (k + 1 < nblk) ? g.diag_cta(k + 1) : -1;
+    if (tid == 0) {
+      // this CTA's panel tiles in increasing i (the right-hand side last)
+      int nm = 0;
+      for (int i = k + 1; i <= nblk; ++i) {
+        int x;
+        if (i == k + 1 && Dn >= 0) {
+          x = Dn;
+        } else {
+          x = (i - k - 2 + C) % (C - 1);
+          if (Dn >= 0 && x >= Dn) ++x;
         }
-        __syncthreads();
-        if (k + 1 < nblk) {
-          const int rr = tid >> 4, cc = tid & 15;
-          for (int i = k + 1; i <= nblk; ++i) {
-            if (g.owner(i, k) != r) continue;
-            const int s = g.slot(i, k);
-            const double wv = sm[g.o_w() + (size_t)s * kTile + tid];
-            const double lv = sm[(size_t)s * kTile + tid];
-            for (int xx = 0; xx < C; ++xx) {
-              const Need nd = s_need[xx];
-              if (i >= nd.rmin && i <= nd.rmax)
-                cl.map_shared_rank(stW, xx)[(size_t)i * kTile + tid] = wv;
-              if (i < nblk && i >= nd.cmin && i <= nd.cmax)
-                cl.map_shared_rank(stL, xx)[(size_t)i * kPadTile + rr * kPad + cc] = lv;
-            }
+        if (x == r) s_mine[nm++] = i;
+      }
+      s_mine[kMaxBlk + 1] = nm;
+    }
+    double a_diag = 0.0;
+    if (r == Dn) a_diag = __ldcg(ws_lower(ws, ld, k + 1, k + 1) + (size_t)rr * ld + cc);
+    __syncthreads();
+    const int mine = s_mine[kMaxBlk + 1];
+    if (mine) {
+      Lkk[rr * kPad + cc] = __ldcg(ws_lower(ws, ld, k, k) + (size_t)rr * ld + cc);
+      if (tid < kB) Lkk[kPadTile + tid] = __ldcg(ws + (size_t)(ld + 1) * ld + kB * k + tid);
+      __syncthreads();
+      // work items (panel tile, row pair); warp w takes items w, w + 8, ...
+      for (int item = warp; item < mine * (kB / 2); item += 8) {
+        const int i = s_mine[item >> 3], p = item & 7;
+        if (i == nblk && p > 0) continue;
+        const int row = 2 * p + (lane >> 4), c = lane & 15;
+        double a = (i < nblk || row == 0) ? __ldcg(ws_tile(ws, ld, nblk, i, k, row, c)) : 0.0;
+#pragma unroll
+        for (int q = 0; q < kB - 1; ++q) {
+          const double wq = __shfl_sync(0xffffffffu, a, (lane & 16) | q);
+          if (c > q) a = fma(-wq, Lkk[c * kPad + q], a);
+        }
+        const double l = a * Lkk[kPadTile + c];
+        if (i < nblk) {
+          ws_lower(ws, ld, i, k)[(size_t)row * ld + c] = a;
+          ws_upper(ws, ld, i, k)[(size_t)row * ld + c] = l;
+          if (i == k + 1 && r == Dn) {
+            stW[(size_t)i * kTile + row * kB + c] = a;
+            stL[(size_t)i * kPadTile + row * kPad + c] = l;
           }
+        } else if (row == 0) {
+          ws[(size_t)ld * ld + kB * k + c] = a;
+          ws[(size_t)(ld + 2) * ld + kB * k + c] = l;
         }
       }
     }
     cl.sync();
     if (k == nblk - 1) break;
 
-    // ---- trailing update of step k from the pushed panel tiles; the owner D
-    //      of diagonal tile k+1 updates and factors it first (look-ahead)
+    // ---- trailing update of step k; D updates and factors tile (k+1, k+1)
+    //      first, then takes its (reduced) range
     const Need nd = trail_need(g, k, r);
-    const int D = g.owner(k + 1, k + 1);
-    const int rr = tid >> 4, cc = tid & 15;
-    if (r == D) {
-      double* A = sm + (size_t)g.slot(k + 1, k + 1) * kTile;
+    if (r == Dn) {
+      // W_{k+1,k} and L_{k+1,k} are already in this CTA's staging area
       const double* wr = stW + (size_t)(k + 1) * kTile + rr * kB;
       const double* lc = stL + (size_t)(k + 1) * kPadTile + cc * kPad;
       double s0 = 0.0, s1 = 0.0;
@@ -310,118 +383,112 @@ __global__ void __launch_bounds__(kThreads) k_ldlt_cluster(const double* __restr
         s0 = fma(wr[q], lc[q], s0);
         s1 = fma(wr[q + 1], lc[q + 1], s1);
       }
-      A[tid] -= s0 + s1;
+      Td[tid] = a_diag - (s0 + s1);
       __syncthreads();
-      const int s = g.slot(k + 1, k + 1);
-      if (tid < 128) diag_ldlt(sm + (size_t)s * kTile, sm + g.o_rd() + (size_t)s * kB, flag0);
+      factor_publish(g, ws, Td, k + 1, solve_ok);
       __syncthreads();
-      push_lkk(cl, sm, g, k + 1);
     }
-    for (int L0 = nd.lo; L0 < nd.hi; L0 += 8) {
-      double av[8];
-      double* ap[8];
+    if (nd.hi > nd.lo) {
+      stage_panel(g, ws, k, nd.rmin, nd.rmax, nd.cmin, nd.cmax, stW, stL);
+      __syncthreads();
+      for (int L0 = nd.lo; L0 < nd.hi; L0 += 8) {
+        double av[8];
+        int ti[8], tj[8];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        ap[u] = nullptr;
-        av[u] = 0.0;
-        const int L = L0 + u;
-        if (L < nd.hi) {
-          int i, j;
-          trail_ij(g, k, L, i, j);
-          if (i < nblk || rr == 0) {
-            ap[u] = cl.map_shared_rank(sm + (size_t)g.slot(i, j) * kTile, g.owner(i, j)) + tid;
-            av[u] = *ap[u];
+        for (int u = 0; u < 8; ++u) {
+          av[u] = 0.0;
+          ti[u] = -1;
+          const int L = L0 + u;
+          if (L < nd.hi) {
+            trail_ij(g, k, L, ti[u], tj[u]);
+            if ((ti[u] < nblk || rr == 0) && !(ti[u] == tj[u] && rr < cc))
+              av[u] = __ldcg(ws_tile(ws, ld, nblk, ti[u], tj[u], rr, cc));
           }
         }
-      }
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int L = L0 + u;
-        if (L >= nd.hi || !ap[u]) continue;
-        int i, j;
-        trail_ij(g, k, L, i, j);
-        const double* wr = stW + (size_t)i * kTile + rr * kB;
-        const double* lc = stL + (size_t)j * kPadTile + cc * kPad;
-        double s0 = 0.0, s1 = 0.0;
+        for (int u = 0; u < 8; ++u) {
+          // right-hand-side tiles have only row 0; diagonal tiles are read
+          // only on and below the diagonal
+          if (ti[u] < 0 || (ti[u] == nblk && rr != 0) || (ti[u] == tj[u] && rr < cc)) continue;
+          const double* wr = stW + (size_t)ti[u] * kTile + rr * kB;
+          const double* lc = stL + (size_t)tj[u] * kPadTile + cc * kPad;
+          double s0 = 0.0, s1 = 0.0;
 #pragma unroll
-        for (int q = 0; q < kB; q += 2) {
-          s0 = fma(wr[q], lc[q], s0);
-          s1 = fma(wr[q + 1], lc[q + 1], s1);
+          for (int q = 0; q < kB; q += 2) {
+            s0 = fma(wr[q], lc[q], s0);
+            s1 = fma(wr[q + 1], lc[q + 1], s1);
+          }
+          __stcg(ws_tile(ws, ld, nblk, ti[u], tj[u], rr, cc), av[u] - (s0 + s1));
         }
-        *ap[u] = av[u] - (s0 + s1);
       }
     }
     cl.sync();
   }
 
-  // ---- backward solve L^T x = y (y: row 0 of the right-hand-side tiles) on
-  //      CTA 0, which streams block row J-1 of L in while it works on row J
-  // every CTA reads CTA 0's flag before any CTA may leave (a CTA's shared
-  // memory must not be read remotely once it has exited)
-  const int failed = *flag0;
-  cl.sync();
-  if (failed) {
-    if (r == 0 && tid == 0) *solve_ok = 0;
-    return;  // no CTA touches distributed shared memory after this point
-  }
-  if (r == 0) {
-    double* t = sm + g.o_t();
-    double* buf[2] = {stW, stL};  // row buffers (nblk tiles each)
-    for (int e = tid; e < kB * nblk; e += kThreads) {
-      const int I = e >> 4;
-      t[e] = cl.map_shared_rank(sm + (size_t)g.slot(nblk, I) * kTile, g.owner(nblk, I))[e & 15];
+  // ---- backward solve L^T x = y on CTA 0 from the workspace; block row
+  //      J-1 of L is staged while row J is worked on
+  if (r != 0) return;
+  if (!*(volatile int*)solve_ok) return;
+  double* t = sm + g.o_t();
+  double* buf[2] = {sm + g.o_buf(), sm + g.o_buf() + (size_t)nblk * kTile};
+  for (int e = tid; e < kB * nblk; e += kThreads) t[e] = __ldcg(ws + (size_t)(ld + 2) * ld + e);
+  // block row J of L: L_JJ (strict lower, diagonal tile) and L_JI, I < J;
+  // threads [t0, 256) copy it
+  auto stage_row = [&](int J, double* dst, int t0) {
+    const int step = kThreads - t0, n = (J + 1) * kTile;
+    for (int e0 = tid - t0; e0 < n; e0 += 8 * step) {
+      double v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = e0 + u * step;
+        v[u] = 0.0;
+        if (e < n) {
+          const int I = e >> 8, q = e & 255;
+          const double* src = (I == J) ? ws_lower(ws, ld, J, J) : ws_upper(ws, ld, J, I);
+          v[u] = __ldcg(src + (size_t)(q >> 4) * ld + (q & 15));
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (e0 + u * step < n) dst[e0 + u * step] = v[u];
     }
-    for (int I = 0; I < nblk; ++I)  // row nblk-1
-      buf[(nblk - 1) & 1][(size_t)I * kTile + tid] =
-          cl.map_shared_rank(sm + (size_t)g.slot(nblk - 1, I) * kTile, g.owner(nblk - 1, I))[tid];
+  };
+  stage_row(nblk - 1, buf[(nblk - 1) & 1], 0);
+  __syncthreads();
+  for (int J = nblk - 1; J >= 0; --J) {
+    const double* Lr = buf[J & 1];
+    if (warp == 0) {
+      // x_J: unit upper solve L_JJ^T x_J = t_J
+      const int c = lane & 15;
+      double tc = t[kB * J + c];
+      const double* Ljj = Lr + (size_t)J * kTile;
+#pragma unroll
+      for (int q = kB - 1; q >= 0; --q) {
+        const double xq = __shfl_sync(0xffffffffu, tc, q);
+        if (c < q) tc = fma(-Ljj[q * kB + c], xq, tc);
+      }
+      if (lane < kB) {
+        s_x[lane] = tc;
+        if (kB * J + lane < n) x[kB * J + lane] = tc;
+      }
+    } else if (J >= 1) {
+      stage_row(J - 1, buf[(J - 1) & 1], 32);  // meanwhile the other warps stage row J-1
+    }
     __syncthreads();
-    for (int J = nblk - 1; J >= 0; --J) {
-      const double* Lr = buf[J & 1];
-      // prefetch row J-1 into registers
-      double pre[kMaxBlk];
+    // t_I -= L_JI^T x_J, I < J
+    for (int it = tid; it < kB * J; it += kThreads) {
+      const int I = it >> 4, c = it & 15;
+      const double* T = Lr + (size_t)I * kTile;
+      double v0 = 0.0, v1 = 0.0;
 #pragma unroll
-      for (int I = 0; I < kMaxBlk; ++I)
-        pre[I] = (J >= 1 && I <= J - 1)
-                     ? cl.map_shared_rank(sm + (size_t)g.slot(J - 1, I) * kTile, g.owner(J - 1, I))[tid]
-                     : 0.0;
-      // x_J: unit upper solve L_JJ^T x_J = t_J, one warp
-      if (warp == 0) {
-        const int c = lane & 15;
-        double tc = t[kB * J + c];
-        const double* Ljj = Lr + (size_t)J * kTile;
-#pragma unroll
-        for (int q = kB - 1; q >= 0; --q) {
-          const double xq = __shfl_sync(0xffffffffu, tc, q);
-          if (c < q) tc = fma(-Ljj[q * kB + c], xq, tc);
-        }
-        if (lane < kB) {
-          s_x[lane] = tc;
-          if (kB * J + lane < n) x[kB * J + lane] = tc;
-        }
+      for (int q = 0; q < kB; q += 2) {
+        v0 = fma(T[q * kB + c], s_x[q], v0);
+        v1 = fma(T[(q + 1) * kB + c], s_x[q + 1], v1);
       }
-      __syncthreads();
-      // t_I -= L_JI^T x_J, I < J
-      for (int it = tid; it < kB * J; it += kThreads) {
-        const int I = it >> 4, c = it & 15;
-        const double* T = Lr + (size_t)I * kTile;
-        double v0 = 0.0, v1 = 0.0;
-#pragma unroll
-        for (int q = 0; q < kB; q += 2) {
-          v0 = fma(T[q * kB + c], s_x[q], v0);
-          v1 = fma(T[(q + 1) * kB + c], s_x[q + 1], v1);
-        }
-        t[kB * I + c] -= v0 + v1;
-      }
-      if (J >= 1) {
-        double* nb = buf[(J - 1) & 1];
-#pragma unroll
-        for (int I = 0; I < kMaxBlk; ++I)
-          if (I <= J - 1) nb[(size_t)I * kTile + tid] = pre[I];
-      }
-      __syncthreads();
+      t[kB * I + c] -= v0 + v1;
     }
+    __syncthreads();
   }
-  cl.sync();  // every CTA keeps its shared memory until CTA 0 is done
 }
 
 Geo make_geo(int C, int ld, int n) {
@@ -430,7 +497,6 @@ Geo make_geo(int C, int ld, int n) {
   g.nblk = (n + kB - 1) / kB;
   g.ld = ld;
   g.n = n;
-  g.nslots = (g.ntiles() + C - 1) / C;
   return g;
 }
 
@@ -478,8 +544,8 @@ int chol_cluster_plan(int ld, int n, CholPlan* plan) {
   return 0;
 }
 
-cudaError_t chol_cluster_launch(const CholPlan& plan, const double* S, int ld, int n, double* x, int* solve_ok,
-                                cudaStream_t st) {
+cudaError_t chol_cluster_launch(const CholPlan& plan, const double* S, double* ws, int ld, int n, double* x,
+                                int* solve_ok, cudaStream_t st) {
   const Geo g = make_geo(plan.cluster, ld, n);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(plan.cluster, 1, 1);
@@ -493,7 +559,7 @@ cudaError_t chol_cluster_launch(const CholPlan& plan, const double* S, int ld, i
   attr.val.clusterDim.z = 1;
   cfg.attrs = &attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, k_ldlt_cluster, S, ld, n, x, solve_ok, g);
+  return cudaLaunchKernelEx(&cfg, k_ldlt_cluster, S, ws, ld, n, x, solve_ok, g);
 }
 
 }  // namespace mcba

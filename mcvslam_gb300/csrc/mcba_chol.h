@@ -19,8 +19,9 @@ int chol_cluster_plan(int ld, int n, CholPlan* plan);
 
 // Factorises S (row-major, ld columns, identity padding beyond n, b_schur as
 // row ld), solves S x = b and writes x[0..n) -- or sets *solve_ok = 0 and
-// leaves x untouched when a pivot is not positive.
-cudaError_t chol_cluster_launch(const CholPlan& plan, const double* S, int ld, int n, double* x, int* solve_ok,
-                                cudaStream_t st);
+// leaves x untouched when a pivot is not positive.  S is only read; ws is a
+// workspace of (ld + 32) x ld doubles through which the CTAs exchange tiles.
+cudaError_t chol_cluster_launch(const CholPlan& plan, const double* S, double* ws, int ld, int n, double* x,
+                                int* solve_ok, cudaStream_t st);
 
 }  // namespace mcba

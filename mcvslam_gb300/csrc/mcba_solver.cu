@@ -101,6 +101,7 @@ struct Bufs {
   void* ppart;      // [npchunk][36] accumulators
   void* qpart;      // [nchunk][6] accumulators of Hpl Dinv b_l per pose chunk
   double* S;        // [(ld+32) x ld]
+  double* cws;      // [(ld+32) x ld] workspace of the cluster factorisation
   double* dinv;     // [ld] reciprocal Cholesky diagonal
   double* x;        // [6Kf + 3Lf]
   double* cost_part;
@@ -950,7 +951,7 @@ class Solver {
   DBuf<int2> pairs;
   // numerics
   DBuf<char> rows, partials, Hll, bl, yq, ppart, qpart;
-  DBuf<double> Hpp, bp, S, dinv, x, cost_part, scale_part, chi2_out;
+  DBuf<double> Hpp, bp, S, cws, dinv, x, cost_part, scale_part, chi2_out;
   DBuf<LMState> lm;
   DBuf<mcba_trial_log> log;
   LMState* lm_host = nullptr;
@@ -996,7 +997,7 @@ class Solver {
     if (stream) cudaStreamSynchronize(stream);
     graph_release();
     DBuf<double>* ds[] = {&pose_qt[0], &pose_qt[1], &Xd[0], &Xd[1], &pose_qt0, &Xd0,
-                          &Hpp, &bp, &S, &dinv, &x, &cost_part, &scale_part, &chi2_out};
+                          &Hpp, &bp, &S, &cws, &dinv, &x, &cost_part, &scale_part, &chi2_out};
     for (auto* d : ds) d->release();
     pd[0].release();
     pd[1].release();
@@ -1261,6 +1262,7 @@ Bufs make_bufs(Solver* s) {
   B.ppart = s->ppart.p;
   B.qpart = s->qpart.p;
   B.S = s->S.p;
+  B.cws = s->cws.p;
   B.dinv = s->dinv.p;
   B.x = s->x.p;
   B.cost_part = s->cost_part.p;
@@ -1353,7 +1355,7 @@ void launch_trial(Solver* s, const Bufs& B, const Launch& L, PhaseClock& pc, cud
     });
     pc.run(MCBA_PHASE_CHOLESKY, [&] {
       if (s->chol.ok) {
-        chol_cluster_launch(s->chol, B.S, L.ld, L.n, B.x, &B.lm->solve_ok, st);
+        chol_cluster_launch(s->chol, B.S, B.cws, L.ld, L.n, B.x, &B.lm->solve_ok, st);
         s->launches++;
         return;
       }
@@ -1373,6 +1375,12 @@ void launch_trial(Solver* s, const Bufs& B, const Launch& L, PhaseClock& pc, cud
         }
       }
       k_chol_backsolve<<<1, 256, 0, st>>>(B.S, B.dinv, L.ld, L.n, B.x, B.lm);
+      s->launches++;
+      // the tiled factorisation works in place and fills absent blocks in;
+      // the next trial's assembly writes only the present blocks, so S
+      // returns to zeros (identity padding) here
+      const size_t total = (size_t)(L.ld + kNB) * L.ld;
+      k_init_S<<<(int)std::min<size_t>((total + 255) / 256, 4096), 256, 0, st>>>(B.S, L.ld, L.n, total);
       s->launches++;
     });
   }
@@ -1404,6 +1412,7 @@ int alloc_numerics(Solver* s, std::string* err) {
   CK(s->ppart.ensure(std::max<size_t>(1, (size_t)L.npc * 36 * ab)));
   CK(s->qpart.ensure(std::max<size_t>(1, (size_t)L.nchunk * 6 * ab)));
   CK(s->S.ensure((size_t)(L.ld + kNB) * L.ld));
+  CK(s->cws.ensure((size_t)(L.ld + kNB) * L.ld));
   CK(s->dinv.ensure(L.ld));
   CK(s->x.ensure(std::max(nx, 1)));
   CK(s->cost_part.ensure(L.ncost));

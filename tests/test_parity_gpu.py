@@ -278,3 +278,19 @@ def test_indefinite_reduced_system_follows_oracle(precision, gpu):
     np.testing.assert_array_equal(log["accepted"], o["log"]["accepted"])
     if precision == "fp64":
         compare_logs(log, o["log"])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_large_corridor_window_uses_tiled_solve_and_follows_oracle(precision, gpu):
+    # 70 free keyframes (reduced system 420 > 384: the tiled factorisation),
+    # corridor layout so many keyframe pairs share no point: the reduced
+    # matrix has absent blocks, which every trial must see as zeros again
+    pr = synth.local_ba(72, 72 * 60, seed=77, corridor=True)
+    o = oracle.optimize(pr, 6)
+    g = ba.solve(pr, 6, precision)
+    if precision == "fp64":
+        assert g["stats"]["iterations"] == o["ret"]
+        compare_logs(g["log"], o["log"])
+        compare_state(g, o, pr)
+    else:
+        assert abs(g["stats"]["final_chi2"] - o["final_chi2"]) <= 1e-4 * o["final_chi2"]
