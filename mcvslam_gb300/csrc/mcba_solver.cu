@@ -674,9 +674,8 @@ __global__ void __launch_bounds__(256) k_chol_backsolve(const double* S, const d
 // Landmark back-substitution (block_solver.hpp:420-446) and point update,
 // plus the point part of computeScale (optimization_algorithm_levenberg.cpp:159-165).
 template <typename R>
-__global__ void k_backsub(Bufs B, int Lf, int n) {
-  __shared__ double sh[32];
-  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void backsub_block(const Bufs& B, int Lf, int n, int blk, double* sh) {
+  const int l = blk * blockDim.x + threadIdx.x;
   const int cur = B.lm->cur, cand = cur ^ 1;
   const double lam = B.lm->lambda;
   double sc = 0.0;
@@ -720,15 +719,14 @@ __global__ void k_backsub(Bufs B, int Lf, int n) {
     B.Xf[cand][id] = make_float4((float)nx[0], (float)nx[1], (float)nx[2], 0.f);
   }
   const double tot = block_sum(sc, sh);
-  if (threadIdx.x == 0) B.scale_part[blockIdx.x] = tot;
+  if (threadIdx.x == 0) B.scale_part[blk] = tot;
 }
 
 // VertexSE3Expmap::oplusImpl on every free pose into the candidate buffer,
 // plus the pose part of computeScale.  Written to scale_part[slot].
 template <typename R>
-__global__ void k_update_poses(Bufs B, int Kf, int slot0) {
-  __shared__ double sh[32];
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void update_poses_block(const Bufs& B, int Kf, int slot0, int blk, double* sh) {
+  const int i = blk * blockDim.x + threadIdx.x;
   const int cur = B.lm->cur, cand = cur ^ 1;
   const double lam = B.lm->lambda;
   double sc = 0.0;
@@ -760,7 +758,20 @@ __global__ void k_update_poses(Bufs B, int Kf, int slot0) {
     for (int k = 0; k < 6; ++k) sc += u[k] * (lam * u[k] + B.bp[6 * (size_t)i + k]);
   }
   const double tot = block_sum(sc, sh);
-  if (threadIdx.x == 0) B.scale_part[slot0 + blockIdx.x] = tot;
+  if (threadIdx.x == 0) B.scale_part[slot0 + blk] = tot;
+}
+
+// One launch for both updates: the pose blocks (long FP64 exp chains) come
+// first so that they start early and overlap the point blocks.  Scale
+// partials keep their slots (points first, then poses), so the sum order
+// does not depend on the launch layout.
+template <typename R>
+__global__ void k_update(Bufs B, int Lf, int n, int Kf, int npose_blocks, int npt_blocks) {
+  __shared__ double sh[32];
+  if ((int)blockIdx.x < npose_blocks)
+    update_poses_block<R>(B, Kf, npt_blocks, blockIdx.x, sh);
+  else
+    backsub_block<R>(B, Lf, n, blockIdx.x - npose_blocks, sh);
 }
 
 // activeRobustChi2 (sparse_optimizer.cpp:102-116) at the current (which = 0)
@@ -796,10 +807,6 @@ __global__ void k_lm_begin(Bufs B, int ncost) {
     B.lm->current_chi = c;
     B.lm->initial_chi = c;
   }
-}
-
-__global__ void k_trial_begin(LMState* lm) {
-  if (threadIdx.x == 0) lm->solve_ok = 1;
 }
 
 // One LM trial's decision (optimization_algorithm_levenberg.cpp:113-141).
@@ -859,6 +866,9 @@ __global__ void k_lm_decide(Bufs B, int ncost, int nscale, cudaGraphConditionalH
     if (lm->trial == lm->max_trials || rho == 0 || !isfinite(lm->lambda)) lm->terminate = 1;
     lm->iteration++;
   }
+  // the next trial starts from a successful solve until the factorisation
+  // says otherwise
+  lm->solve_ok = 1;
   if (in_graph) cudaGraphSetConditional(h_trial, more ? 1u : 0u);
 }
 
@@ -1336,8 +1346,6 @@ template <typename R>
 void launch_trial(Solver* s, const Bufs& B, const Launch& L, PhaseClock& pc, cudaGraphConditionalHandle h_trial,
                   int in_graph) {
   cudaStream_t st = s->stream;
-  k_trial_begin<<<1, 32, 0, st>>>(B.lm);
-  s->launches++;
   if (L.Kf) {
     pc.run(MCBA_PHASE_SCHUR_EDGE, [&] {
       k_schur_edge<R><<<L.nchunk, kLinThreads, 0, st>>>(B);
@@ -1385,9 +1393,8 @@ void launch_trial(Solver* s, const Bufs& B, const Launch& L, PhaseClock& pc, cud
     });
   }
   pc.run(MCBA_PHASE_UPDATE, [&] {
-    k_backsub<R><<<L.nscale_pts, 128, 0, st>>>(B, L.Lf, L.n);
-    k_update_poses<R><<<L.nscale_pose, 128, 0, st>>>(B, L.Kf, L.nscale_pts);
-    s->launches += 2;
+    k_update<R><<<L.nscale_pose + L.nscale_pts, 128, 0, st>>>(B, L.Lf, L.n, L.Kf, L.nscale_pose, L.nscale_pts);
+    s->launches += 1;
   });
   pc.run(MCBA_PHASE_COST, [&] {
     k_cost<R><<<L.ncost, 256, 0, st>>>(B, L.E, 1);
