@@ -300,9 +300,7 @@ __global__ void __launch_bounds__(kLinThreads) k_linearize(Bufs B) {
 // Hpp / b_p: sum of the chunk partials of each free pose (warp per pose),
 // stored in FP64.
 template <typename R>
-__global__ void k_pose_reduce(Bufs B, int Kf) {
-  const int i = blockIdx.x;
-  const int lane = threadIdx.x;
+__device__ __forceinline__ void pose_reduce_warp(const Bufs& B, int Kf, int i, int lane) {
   if (i >= Kf) return;
   const int c0 = B.pose_chunk_begin[i], c1 = B.pose_chunk_begin[i + 1];
   const Acc<R>* part = reinterpret_cast<const Acc<R>*>(B.partials);
@@ -327,8 +325,7 @@ __global__ void k_pose_reduce(Bufs B, int Kf) {
 
 // Hll / b_l: sum over the (<= a few) edges of each free point.
 template <typename R>
-__global__ void k_point_reduce(Bufs B, int Lf, int n) {
-  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void point_reduce_thread(const Bufs& B, int Lf, int l) {
   if (l >= Lf) return;
   const int e0 = B.pt_begin[l], e1 = B.pt_begin[l + 1];
   R s[9];
@@ -345,6 +342,17 @@ __global__ void k_point_reduce(Bufs B, int Lf, int n) {
   R* b = Ptrs<R>::p(B.bl) + 3 * (size_t)l;
 #pragma unroll
   for (int k = 0; k < 3; ++k) b[k] = s[6 + k];
+}
+
+// Both reductions in one launch of 128-thread blocks: the first blocks take
+// four free poses each (a warp per pose), the rest 128 free points each.
+template <typename R>
+__global__ void k_reduce(Bufs B, int Kf, int Lf, int npose_blocks) {
+  const int blk = blockIdx.x;
+  if (blk < npose_blocks)
+    pose_reduce_warp<R>(B, Kf, 4 * blk + (threadIdx.x >> 5), threadIdx.x & 31);
+  else
+    point_reduce_thread<R>(B, Lf, (blk - npose_blocks) * blockDim.x + threadIdx.x);
 }
 
 // computeLambdaInit (optimization_algorithm_levenberg.cpp:145-157):
@@ -1325,12 +1333,9 @@ void launch_linearize(Solver* s, const Bufs& B, const Launch& L, bool first, dou
     s->launches++;
   });
   pc.run(MCBA_PHASE_REDUCE, [&] {
-    if (L.Kf) {
-      k_pose_reduce<R><<<L.Kf, 32, 0, st>>>(B, L.Kf);
-      s->launches++;
-    }
-    if (L.Lf) {
-      k_point_reduce<R><<<(L.Lf + 127) / 128, 128, 0, st>>>(B, L.Lf, L.n);
+    if (L.Kf || L.Lf) {
+      const int npb = (L.Kf + 3) / 4;
+      k_reduce<R><<<npb + (L.Lf + 127) / 128, 128, 0, st>>>(B, L.Kf, L.Lf, npb);
       s->launches++;
     }
     if (first) {
