@@ -13,11 +13,13 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
 
 #include "mcba.h"
+#include "mcba_host_pool.h"
 #include "mcba_internal.h"
 
 namespace mcba {
@@ -429,11 +431,28 @@ void mcba_default_options(mcba_options* o) {
   o->host_structure = 0;
 }
 
+namespace {
+// Host-side problem storage of destroyed handles, kept (cleared, with its
+// capacity) for the next handle: a caller that creates a handle per solve
+// then loads into memory that is already mapped.
+std::mutex g_hp_mu;
+std::vector<HostProblem> g_hp_pool;
+constexpr size_t kHostPoolMax = 4;
+}  // namespace
+
 int mcba_create(const mcba_options* opt, mcba_problem** out) {
   if (!out) return MCBA_ERR_INVALID;
   *out = nullptr;
   mcba_problem* p = new (std::nothrow) mcba_problem();
   if (!p) return MCBA_ERR_NOMEM;
+  {
+    std::lock_guard<std::mutex> lk(g_hp_mu);
+    if (!g_hp_pool.empty()) {
+      p->hp = std::move(g_hp_pool.back());
+      g_hp_pool.pop_back();
+      p->hp.clear();
+    }
+  }
   if (opt) {
     p->opt = *opt;
   } else {
@@ -452,6 +471,10 @@ int mcba_create(const mcba_options* opt, mcba_problem** out) {
 int mcba_destroy(mcba_problem* p) {
   if (!p) return MCBA_ERR_INVALID;
   if (p->solver) solver_destroy(p->solver);
+  {
+    std::lock_guard<std::mutex> lk(g_hp_mu);
+    if (g_hp_pool.size() < kHostPoolMax) g_hp_pool.push_back(std::move(p->hp));
+  }
   delete p;
   return MCBA_OK;
 }
@@ -614,39 +637,81 @@ int mcba_load(mcba_problem* p, const mcba_problem_desc* d) {
   }
   const size_t E = d->n_edges;
   const int K = d->n_poses, P = d->n_points, C = d->n_cams;
-  // bulk copies, then one branch-free validation pass (the failing edge is
-  // looked up only when the pass reports a problem)
-  h.e_type.assign(d->edge_type, d->edge_type + E);
-  h.e_pose.assign(d->edge_pose, d->edge_pose + E);
-  h.e_point.assign(d->edge_point, d->edge_point + E);
-  h.e_cam.assign(d->edge_cam, d->edge_cam + E);
-  h.e_obs.assign(d->edge_obs, d->edge_obs + 3 * E);
-  if (d->edge_info) h.e_info.assign(d->edge_info, d->edge_info + E);
-  else h.e_info.assign(E, 1.f);
-  if (d->edge_delta) h.e_delta.assign(d->edge_delta, d->edge_delta + E);
-  else h.e_delta.assign(E, 0.f);
-  h.e_robust.resize(E);
-  if (d->edge_robust)
-    for (size_t i = 0; i < E; ++i) h.e_robust[i] = d->edge_robust[i] ? 1 : 0;
-  else
-    std::fill(h.e_robust.begin(), h.e_robust.end(), (uint8_t)1);
-  if (d->edge_level) h.e_level.assign(d->edge_level, d->edge_level + E);
-  else h.e_level.assign(E, 0);
-  auto nonfinite = [](float v) {
-    uint32_t b;
-    std::memcpy(&b, &v, 4);
-    return (b & 0x7f800000u) == 0x7f800000u;
+  // bulk copies (one array per pool task), then branch-free validation of
+  // contiguous edge ranges in parallel (the failing edge is looked up only
+  // when a range reports a problem)
+  HostPool& pool = HostPool::get();
+  pool.run(9, [&](int task) {
+    switch (task) {
+      case 0: h.e_type.assign(d->edge_type, d->edge_type + E); break;
+      case 1: h.e_pose.assign(d->edge_pose, d->edge_pose + E); break;
+      case 2: h.e_point.assign(d->edge_point, d->edge_point + E); break;
+      case 3: h.e_cam.assign(d->edge_cam, d->edge_cam + E); break;
+      case 4: h.e_obs.assign(d->edge_obs, d->edge_obs + 3 * E); break;
+      case 5:
+        if (d->edge_info) h.e_info.assign(d->edge_info, d->edge_info + E);
+        else h.e_info.assign(E, 1.f);
+        break;
+      case 6:
+        if (d->edge_delta) h.e_delta.assign(d->edge_delta, d->edge_delta + E);
+        else h.e_delta.assign(E, 0.f);
+        break;
+      case 7:
+        h.e_robust.resize(E);
+        if (d->edge_robust)
+          for (size_t i = 0; i < E; ++i) h.e_robust[i] = d->edge_robust[i] ? 1 : 0;
+        else
+          std::fill(h.e_robust.begin(), h.e_robust.end(), (uint8_t)1);
+        break;
+      default:
+        if (d->edge_level) h.e_level.assign(d->edge_level, d->edge_level + E);
+        else h.e_level.assign(E, 0);
+        break;
+    }
+  });
+  // one simple loop per array, branch-free, so that each vectorises
+  auto nonfinite_any = [](const float* v, size_t n) {
+    const uint32_t* b = reinterpret_cast<const uint32_t*>(v);
+    uint32_t bad = 0;
+    for (size_t i = 0; i < n; ++i) bad |= (uint32_t)((b[i] & 0x7f800000u) == 0x7f800000u);
+    return bad;
   };
+  auto out_of_range = [](const int32_t* v, size_t n, int lim) {
+    const uint32_t* u = reinterpret_cast<const uint32_t*>(v);
+    uint32_t bad = 0;
+    for (size_t i = 0; i < n; ++i) bad |= (uint32_t)(u[i] >= (uint32_t)lim);
+    return bad;
+  };
+  constexpr int kParts = 16;
+  unsigned flags[kParts][4] = {};
+  size_t nun[kParts] = {};
+  const size_t per = (E + kParts - 1) / kParts;
+  pool.run(E >= 4096 ? kParts : 1, [&](int q) {
+    const size_t b = (E >= 4096) ? (size_t)q * per : 0, e = (E >= 4096) ? std::min(E, b + per) : E;
+    if (b >= e) return;
+    const size_t n = e - b;
+    unsigned bt = 0;
+    size_t nu = 0;
+    for (size_t i = b; i < e; ++i) {
+      const uint8_t t = h.e_type[i];
+      bt |= (unsigned)(t > MCBA_EDGE_UNARY);
+      nu += (size_t)(t == MCBA_EDGE_UNARY);
+    }
+    flags[q][0] = bt;
+    flags[q][1] = out_of_range(h.e_pose.data() + b, n, K) | out_of_range(h.e_point.data() + b, n, P) |
+                  out_of_range(h.e_cam.data() + b, n, C);
+    flags[q][2] = nonfinite_any(h.e_obs.data() + 3 * b, 3 * n);
+    flags[q][3] = nonfinite_any(h.e_info.data() + b, n) | nonfinite_any(h.e_delta.data() + b, n);
+    nun[q] = nu;
+  });
   unsigned bad_type = 0, bad_index = 0, bad_obs = 0, bad_w = 0;
   size_t n_unary = 0;
-  for (size_t i = 0; i < E; ++i) {
-    const uint8_t t = h.e_type[i];
-    bad_type |= t > MCBA_EDGE_UNARY;
-    bad_index |= (unsigned)h.e_pose[i] >= (unsigned)K || (unsigned)h.e_point[i] >= (unsigned)P ||
-                 (unsigned)h.e_cam[i] >= (unsigned)C;
-    bad_obs |= nonfinite(h.e_obs[3 * i]) | nonfinite(h.e_obs[3 * i + 1]) | nonfinite(h.e_obs[3 * i + 2]);
-    bad_w |= nonfinite(h.e_info[i]) | nonfinite(h.e_delta[i]);
-    n_unary += t == MCBA_EDGE_UNARY;
+  for (int q = 0; q < kParts; ++q) {
+    bad_type |= flags[q][0];
+    bad_index |= flags[q][1];
+    bad_obs |= flags[q][2];
+    bad_w |= flags[q][3];
+    n_unary += nun[q];
   }
   if (bad_type) return fail(p, MCBA_ERR_INVALID, "unknown edge type");
   if (bad_index) return fail(p, MCBA_ERR_INVALID, "edge index out of range");

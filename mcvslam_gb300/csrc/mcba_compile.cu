@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "mcba.h"
+#include "mcba_host_pool.h"
 #include "mcba_internal.h"
 
 namespace mcba {
@@ -567,20 +568,27 @@ int compiler_phase1(DeviceCompiler* c, const HostProblem& hp, cudaStream_t st, S
   }
   if (!c->h_sizes) CK(cudaMallocHost(&c->h_sizes, 16 * sizeof(int)));
   char* h = c->h_stage;
-  if (Eall) {
-    std::memcpy(h + off[0], hp.e_pose.data(), sizes[0]);
-    std::memcpy(h + off[1], hp.e_point.data(), sizes[1]);
-    std::memcpy(h + off[2], hp.e_type.data(), sizes[2]);
-    uint8_t* cam8 = reinterpret_cast<uint8_t*>(h + off[3]);
-    for (int i = 0; i < Eall; ++i) cam8[i] = (uint8_t)hp.e_cam[i];
-    std::memcpy(h + off[4], hp.e_level.data(), sizes[4]);
-    std::memcpy(h + off[5], hp.e_robust.data(), sizes[5]);
-    std::memcpy(h + off[6], hp.e_info.data(), sizes[6]);
-    std::memcpy(h + off[7], hp.e_delta.data(), sizes[7]);
-    std::memcpy(h + off[8], hp.e_obs.data(), sizes[8]);
-  }
-  if (K) std::memcpy(h + off[9], hp.pose_fixed.data(), sizes[9]);
-  if (P) std::memcpy(h + off[10], hp.point_fixed.data(), sizes[10]);
+  // the staging copies, one array per host-pool task
+  HostPool::get().run(11, [&](int a) {
+    if (a < 9 && !Eall) return;
+    switch (a) {
+      case 0: std::memcpy(h + off[0], hp.e_pose.data(), sizes[0]); break;
+      case 1: std::memcpy(h + off[1], hp.e_point.data(), sizes[1]); break;
+      case 2: std::memcpy(h + off[2], hp.e_type.data(), sizes[2]); break;
+      case 3: {
+        uint8_t* cam8 = reinterpret_cast<uint8_t*>(h + off[3]);
+        for (int i = 0; i < Eall; ++i) cam8[i] = (uint8_t)hp.e_cam[i];
+        break;
+      }
+      case 4: std::memcpy(h + off[4], hp.e_level.data(), sizes[4]); break;
+      case 5: std::memcpy(h + off[5], hp.e_robust.data(), sizes[5]); break;
+      case 6: std::memcpy(h + off[6], hp.e_info.data(), sizes[6]); break;
+      case 7: std::memcpy(h + off[7], hp.e_delta.data(), sizes[7]); break;
+      case 8: std::memcpy(h + off[8], hp.e_obs.data(), sizes[8]); break;
+      case 9: if (K) std::memcpy(h + off[9], hp.pose_fixed.data(), sizes[9]); break;
+      default: if (P) std::memcpy(h + off[10], hp.point_fixed.data(), sizes[10]); break;
+    }
+  });
   CK(c->d_raw.ensure(cur));
   CK(cudaMemcpyAsync(c->d_raw.p, h, cur, cudaMemcpyHostToDevice, st));
   if (h2d) *h2d += (int64_t)cur;
