@@ -345,7 +345,7 @@ def run_mcba(args):
         "peak": fp64_peak, "unit": "GFLOP/s", "frac": flops / (chol_ms / 1e3) / 1e9 / fp64_peak,
         "peak_source": "nominal FP64 rate of the part (no measured FP64 figure in MEASURED_PEAKS.json)",
         "ms_per_launch": chol_ms, "n": nred,
-        "chain_floor_us": nred * PIVOT_CHAIN_CYCLES / (clk_mhz_nominal() * 1e-3) if nred else None,
+        "chain_floor_us": nred * PIVOT_CHAIN_CYCLES / clk_mhz_nominal() if nred else None,
         "note": "n^3/3 + 4 n^2 flops per solve; the floor is one dependent FP64 pivot step (about "
                 f"{PIVOT_CHAIN_CYCLES} cycles: FMA plus reciprocal with one Newton step) per unknown"}
 

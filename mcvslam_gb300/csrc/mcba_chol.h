@@ -10,17 +10,20 @@ namespace mcba {
 struct CholPlan {
   bool ok = false;
   int cluster = 0;
+  int slots = 0;  // backward-solve row slots held in shared memory
   size_t smem_bytes = 0;
 };
 
-// Chooses a cluster size (16, else 8) whose distributed shared memory holds
-// the n x n system (row stride ld); returns 0 (plan.ok = false) when none does.
+// Chooses a cluster size (16, else 8) for the n x n system (row stride ld)
+// and the number of backward-solve rows staged in shared memory; returns 0
+// (plan.ok = false) when the system is too large for the cluster solve.
 int chol_cluster_plan(int ld, int n, CholPlan* plan);
 
 // Factorises S (row-major, ld columns, identity padding beyond n, b_schur as
 // row ld), solves S x = b and writes x[0..n) -- or sets *solve_ok = 0 and
 // leaves x untouched when a pivot is not positive.  S is only read; ws is a
-// workspace of (ld + 32) x ld doubles through which the CTAs exchange tiles.
+// workspace of (ld + 32) x ld doubles through which the CTAs exchange tiles
+// and their progress flags.
 cudaError_t chol_cluster_launch(const CholPlan& plan, const double* S, double* ws, int ld, int n, double* x,
                                 int* solve_ok, cudaStream_t st);
 
