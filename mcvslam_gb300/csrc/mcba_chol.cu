@@ -24,7 +24,7 @@
 //     next step needs; the arithmetic warps hand results to it through
 //     arrive/sync barriers and never wait for its stores or fences.
 //   * CTAs 1..C-1 (workers) run every other task in one fixed global order,
-//     dealt round robin: panel solves (i, k) for i >= k+2 and the right-hand
+//     dealt round robin: panel solves (i, k) for i >= k+3 and the right-hand
 //     side, the trailing updates A_ij -= W_ik L_jk^T, and the inverses
 //     M_J = L_JJ^-T for the backward solve.  The order is the right-looking
 //     schedule with lookahead: per step k, the panels, then the updates of
@@ -32,8 +32,12 @@
 //     block column k+3 of step k, then the inverse of diagonal tile k-1.
 //     Every task's inputs come earlier in that order (or from the chain
 //     CTA's step k), so waiting on them in order cannot deadlock.  A
-//     worker's ninth warp stores each result, fences it and releases its
-//     flag while the arithmetic warps go on with the next task.
+//     worker's warps 8 and 9 store each result (fence, flag) and stage the
+//     next task's inputs while warps 0-7 compute.
+//   * Worker 1 runs only block row k+2 of each step k: its panel, then the
+//     updates of its tiles (k+2, k+1) and (k+2, k+2), which it pushes
+//     straight into the chain CTA's shared memory (st.async, counted on an
+//     mbarrier there) as the chain CTA's inputs for step k+1.
 //   * The workspace is tile-major: 16x16 tiles of 2 KB, lower positions for
 //     the working tiles (A, then W = L D after its panel solve), upper
 //     positions (j, i) for L_ij.  Each tile has a version flag: the number of
@@ -66,8 +70,9 @@ namespace {
 namespace cg = cooperative_groups;
 
 constexpr int kB = 16;         // tile edge
-constexpr int kThreads = 288;  // warps 0-7: tile arithmetic; warp 8: copies, fences and flags
+constexpr int kThreads = 320;  // warps 0-7: tile arithmetic; warps 8, 9: copies, fences and flags
 constexpr int kMath = 256;
+constexpr int kPair = kMath + 32;  // the arithmetic warps and one copy warp (producer/consumer barriers)
 constexpr int kTile = kB * kB;
 constexpr int kPad = kB + 1;  // row stride of staged tiles (conflict-free column reads)
 constexpr int kPadTile = kB * kPad;
@@ -77,9 +82,11 @@ constexpr unsigned kSpinLimit = 1u << 21;  // polls per wait (~1 s) before the s
 // named barriers (0 is __syncthreads)
 constexpr int kBarPivot = 1;    // pivot chain and pivot application (160 threads)
 constexpr int kBarMath = 2;     // warps 0-7
-constexpr int kBarPanel = 3;    // chain CTA: panel result ready for warp 8 (288)
-constexpr int kBarOutFull = 4;  // workers: result buffer b ready for warp 8 (288), ids 4, 5
-constexpr int kBarOutFree = 6;  // workers: result buffer b stored (288), ids 6, 7
+constexpr int kBarPanel = 3;    // chain CTA: panel result ready for warp 8
+constexpr int kBarOutFull = 4;  // workers: result buffer b ready for warp 8, ids 4, 5
+constexpr int kBarOutFree = 6;  // workers: result buffer b stored, ids 6, 7
+constexpr int kBarInFull = 8;   // workers: inputs of the next task staged by warp 9, ids 8, 9
+constexpr int kBarInFree = 10;  // workers: stage b read by warps 0-7, ids 10, 11
 
 // Reciprocal of a pivot: rcp.approx.ftz.f64 (relative error ~1e-6), then one
 // cubic Newton-Raphson step y (1 + e + e^2), e = 1 - d y, which leaves an
@@ -138,6 +145,33 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
                : "memory");
 }
 
+// This CTA's shared-memory address of `local`'s offset in cluster CTA `rank`.
+__device__ __forceinline__ unsigned cluster_addr(const void* local, unsigned rank) {
+  unsigned r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(local)), "r"(rank));
+  return r;
+}
+
+// Asynchronous 8-byte store into another CTA's shared memory; its arrival is
+// counted in bytes on an mbarrier of that CTA.
+__device__ __forceinline__ void st_async(unsigned raddr, double v, unsigned rbar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.f64 [%0], %1, [%2];" ::"r"(raddr), "d"(v),
+               "r"(rbar)
+               : "memory");
+}
+
+// Phase test with cluster-scope acquire (for data other CTAs stored).
+__device__ __forceinline__ bool mbar_try_wait_cluster(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, "
+      "p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
   unsigned ok;
   asm volatile(
@@ -169,6 +203,14 @@ __device__ void mbar_wait(uint64_t* bar, unsigned parity, int* abort_word) {
   atomicExch(abort_word, 1);
 }
 
+__device__ void mbar_wait_cluster(uint64_t* bar, unsigned parity, int* abort_word) {
+  for (unsigned it = 0; it < kSpinLimit; ++it) {
+    if (mbar_try_wait_cluster(bar, parity)) return;
+    if ((it & 63u) == 0 && ld_acquire(abort_word) != 0) return;
+  }
+  atomicExch(abort_word, 1);
+}
+
 struct Geo {
   int C, nblk, ld, n, R;  // R: backward-solve row slots in shared memory
   // workspace (doubles): nblk x nblk tiles of 256, then the right-hand-side
@@ -186,26 +228,27 @@ struct Geo {
   __host__ __device__ size_t m_offset() const { return flag_offset() + (((size_t)flag_count() + 63) / 64) * 32; }
   __host__ __device__ size_t ws_doubles() const { return m_offset() + (size_t)nblk * kTile; }
   // chain CTA shared memory (doubles): two diagonal tiles with 1/d and the
-  // squares of the sub-diagonal, the incoming panel tile, W and L of the
-  // panel, the padded copy of L_kk with 1/d
+  // squares of the sub-diagonal (step k factors tile D[k & 1] and receives
+  // the next one in D[(k+1) & 1]), two incoming panel tiles (P[k & 1]), W
+  // and L of the panel, the padded copy of L_kk with 1/d, and the two
+  // mbarriers on which the next step's tiles arrive from a worker
   __host__ __device__ size_t c_diag(int b) const { return (size_t)b * (kTile + 2 * kB); }
-  __host__ __device__ size_t c_p() const { return 2 * (size_t)(kTile + 2 * kB); }
-  __host__ __device__ size_t c_wp() const { return c_p() + kTile; }
+  __host__ __device__ size_t c_p(int b) const { return 2 * (size_t)(kTile + 2 * kB) + (size_t)b * kTile; }
+  __host__ __device__ size_t c_wp() const { return c_p(2); }
   __host__ __device__ size_t c_lp() const { return c_wp() + kPadTile; }
   __host__ __device__ size_t c_lk() const { return c_lp() + kPadTile; }
-  __host__ __device__ size_t c_end() const { return c_lk() + kPadTile + kB; }
+  __host__ __device__ size_t c_rx(int b) const { return c_lk() + kPadTile + kB + b; }
+  __host__ __device__ size_t c_end() const { return c_rx(2); }
   // backward solve, after that: t, x, the slot mbarriers, R row slots
   __host__ __device__ size_t b_t() const { return c_end(); }
   __host__ __device__ size_t b_x() const { return b_t() + (size_t)kB * nblk; }
   __host__ __device__ size_t b_bar() const { return b_x() + (size_t)kB * nblk; }
   __host__ __device__ size_t b_slot(int s) const { return b_bar() + (size_t)((R + 1) & ~1) + (size_t)s * nblk * kTile; }
   __host__ __device__ size_t b_end() const { return b_slot(R); }
-  // worker: staged W and L tiles, the padded L_kk with 1/d, two result
-  // buffers of 512
-  __host__ __device__ size_t w_w() const { return 0; }
-  __host__ __device__ size_t w_l() const { return kPadTile; }
-  __host__ __device__ size_t w_lk() const { return 2 * kPadTile; }
-  __host__ __device__ size_t w_out(int b) const { return 3 * kPadTile + kB + (size_t)b * 2 * kTile; }
+  // worker: two input stages (A, then W or L_kk, then L or 1/d) and two
+  // result buffers of 512
+  __host__ __device__ size_t w_stage(int b) const { return (size_t)b * (kTile + 2 * kPadTile); }
+  __host__ __device__ size_t w_out(int b) const { return w_stage(2) + (size_t)b * 2 * kTile; }
   __host__ __device__ size_t w_end() const { return w_out(2); }
   __host__ __device__ size_t total() const {
     size_t t = c_end();
@@ -224,27 +267,7 @@ __device__ __forceinline__ size_t s_at(int ld, int nblk, int i, int j, int rr, i
 __device__ __forceinline__ size_t w_at(const Geo& g, int i, int j, int rr, int cc) {
   return (i < g.nblk) ? g.tile_off(i, j) + rr * kB + cc : g.rhs_w() + kB * j + cc;
 }
-// L_ij (i > j) in the workspace: the upper tile position (j, i).
-__device__ __forceinline__ size_t l_at(const Geo& g, int i, int j, int rr, int cc) {
-  return g.tile_off(j, i) + rr * kB + cc;
-}
 __device__ __forceinline__ int* flag_at(int* fl, int nblk, int i, int j) { return fl + i * nblk + j; }
-
-// Version v of a tile element: S for v = 0, the workspace after that.
-__device__ __forceinline__ double tile_read(const Geo& g, const double* S, const double* ws, int i, int j, int rr,
-                                            int cc, int v) {
-  return v == 0 ? S[s_at(g.ld, g.nblk, i, j, rr, cc)] : __ldcg(ws + w_at(g, i, j, rr, cc));
-}
-
-// Wait of the arithmetic warps on up to three flags, one spinning thread per
-// warp 0..2, then a barrier of warps 0-7.
-__device__ void math_wait3(int* f0, int v0, int* f1, int v1, int* f2, int v2, int* abort_word) {
-  const int tid = threadIdx.x;
-  if (tid == 0 && f0) wait_ge(f0, v0, abort_word);
-  if (tid == 32 && f1) wait_ge(f1, v1, abort_word);
-  if (tid == 64 && f2) wait_ge(f2, v2, abort_word);
-  bar_sync(kBarMath, kMath);
-}
 
 // Forward substitution of two rows per warp against a unit lower L (padded
 // copy Lk): a_row <- a_row L^-T.  Lanes 0-15 hold row 2w, lanes 16-31 row
@@ -338,7 +361,8 @@ __device__ void chain_cta(const Geo& g, const double* __restrict__ S, double* ws
   int* abort_word = fl + g.abort_index();
   double* const Tb0 = sm + g.c_diag(0);
   double* const Tb1 = sm + g.c_diag(1);
-  double* P = sm + g.c_p();
+  double* const P0 = sm + g.c_p(0);
+  double* const P1 = sm + g.c_p(1);
   double* Wp = sm + g.c_wp();
   double* Lp = sm + g.c_lp();
   double* Lk = sm + g.c_lk();
@@ -357,27 +381,29 @@ __device__ void chain_cta(const Geo& g, const double* __restrict__ S, double* ws
   for (int k = 0; k + 1 < nblk; ++k) {
     double* T = cur ? Tb1 : Tb0;
     double* Q = cur ? Tb0 : Tb1;
-    // ---- (a) factor diagonal tile k; warp 8 fetches tiles (k+1, k) and
-    //      (k+1, k+1) at version k meanwhile
+    double* P = (k & 1) ? P1 : P0;
+    // ---- (a) factor diagonal tile k; meanwhile tiles (k+1, k) and
+    //      (k+1, k+1) at version k arrive in P and Q: pushed by the worker
+    //      that ran their last updates, or, for k = 0, read from S by warp 8
     if (warp < 8) {
       if (warp < 4 || warp == 5) diag_ldlt(T, T + kTile, T + kTile + kB, solve_ok);
-    } else {
+    } else if (warp == 8) {
       if (k > 0) {
-        if (lane == 0) wait_ge(flag_at(fl, nblk, k + 1, k), k, abort_word);
-        if (lane == 1) wait_ge(flag_at(fl, nblk, k + 1, k + 1), k, abort_word);
-        __syncwarp();
-      }
-      double v[16];
+        mbar_wait_cluster(reinterpret_cast<uint64_t*>(sm + g.c_rx(k & 1)), (unsigned)(((k - 1) >> 1) & 1),
+                          abort_word);  // rx[1] serves steps 1, 3, .., rx[0] steps 2, 4, ..
+      } else {
+        double v[16];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int e = lane + 32 * u;
-        v[u] = tile_read(g, S, ws, k + 1, k, e >> 4, e & 15, k);
-        v[8 + u] = tile_read(g, S, ws, k + 1, k + 1, e >> 4, e & 15, k);
-      }
+        for (int u = 0; u < 8; ++u) {
+          const int e = lane + 32 * u;
+          v[u] = S[s_at(ld, nblk, 1, 0, e >> 4, e & 15)];
+          v[8 + u] = S[s_at(ld, nblk, 1, 1, e >> 4, e & 15)];
+        }
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        P[lane + 32 * u] = v[u];
-        Q[lane + 32 * u] = v[8 + u];
+        for (int u = 0; u < 8; ++u) {
+          P[lane + 32 * u] = v[u];
+          Q[lane + 32 * u] = v[8 + u];
+        }
       }
     }
     __syncthreads();
@@ -393,9 +419,14 @@ __device__ void chain_cta(const Geo& g, const double* __restrict__ S, double* ws
       const double a = fwd_rows(P[row * kB + c], Lk, lane);
       Wp[row * kPad + c] = a;
       Lp[row * kPad + c] = a * Lk[kPadTile + c];
-      bar_arrive(kBarPanel, kThreads);
+      bar_arrive(kBarPanel, kPair);
       bar_sync(kBarMath, kMath);  // (c) reads rows of W and L written by other warps
-    } else {
+    } else if (warp == 8) {
+      // the bytes step k+1 receives are expected before the flag below lets
+      // the worker push them: two tiles, or the right-hand-side row
+      if (lane == 0)
+        mbar_expect_tx(reinterpret_cast<uint64_t*>(sm + g.c_rx((k + 1) & 1)),
+                       (k + 2 < nblk ? 2 * kTile : kB) * (unsigned)sizeof(double));
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int e = lane + 32 * u;
@@ -405,7 +436,7 @@ __device__ void chain_cta(const Geo& g, const double* __restrict__ S, double* ws
       __threadfence();
       __syncwarp();
       if (lane == 0) st_release(flag_at(fl, nblk, k, k), k + 1);
-      bar_sync(kBarPanel, kThreads);
+      bar_sync(kBarPanel, kPair);
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int e = lane + 32 * u, r0 = e >> 4, c0 = e & 15;
@@ -438,12 +469,16 @@ __device__ void chain_cta(const Geo& g, const double* __restrict__ S, double* ws
   {
     const int k = nblk - 1;
     double* T = cur ? Tb1 : Tb0;
+    double* P = (k & 1) ? P1 : P0;
     if (warp < 8) {
       if (warp < 4 || warp == 5) diag_ldlt(T, T + kTile, T + kTile + kB, solve_ok);
-    } else {
-      if (k > 0 && lane == 0) wait_ge(flag_at(fl, nblk, nblk, k), k, abort_word);
-      __syncwarp();
-      if (lane < kB) P[lane] = tile_read(g, S, ws, nblk, k, 0, lane, k);
+    } else if (warp == 8) {
+      if (k > 0) {
+        mbar_wait_cluster(reinterpret_cast<uint64_t*>(sm + g.c_rx(k & 1)), (unsigned)(((k - 1) >> 1) & 1),
+                          abort_word);
+      } else if (lane < kB) {
+        P[lane] = S[s_at(ld, nblk, nblk, 0, 0, lane)];
+      }
     }
     __syncthreads();
     if (tid < kMath) {
@@ -455,7 +490,7 @@ __device__ void chain_cta(const Geo& g, const double* __restrict__ S, double* ws
       const int row = 2 * warp + (lane >> 4), c = lane & 15;
       const double m = fwd_rows(row == c ? 1.0 : 0.0, Lk, lane);
       slot(k)[k * kTile + c * kB + row] = m;  // M_k stored transposed
-    } else {
+    } else if (warp == 8) {
       const double a = fwd_rows(lane < kB ? P[lane] : 0.0, Lk, lane);
       if (lane < kB) t[kB * k + lane] = a * Lk[kPadTile + lane];
     }
@@ -547,28 +582,177 @@ __device__ void chain_cta(const Geo& g, const double* __restrict__ S, double* ws
 
 // --------------------------------------------------------------- workers --
 //
-// Warps 0-7 run each task into result buffer b (tasks alternate between two
-// buffers); warp 8 then stores the result, fences it and releases its flag.
-// Task kinds and what warp 8 stores:
-//   panel (i, k): W to tile (i, k), L to tile (k, i) (the right-hand side:
-//                 the W and y rows), flag (i, k) = k+1
-//   update (i, j, s): tile (i, j) (lower part of a diagonal tile, row 0 of
-//                 the right-hand side), flag (i, j) = s+1
-//   inverse J:    M_J, inverse flag J = 1
-enum : int { kTaskPanel = 0, kTaskUpdate = 1, kTaskInv = 2 };
+// A worker runs its tasks as a three-stage pipeline: warp 9 waits for a
+// task's inputs and stages them in shared memory (stage b = task parity),
+// warps 0-7 compute the result into result buffer b, and warp 8 stores the
+// result, fences it and releases its flag.  So flag waits, L2 loads and
+// fences overlap the arithmetic of the neighbouring tasks.  Task kinds:
+//   panel (i, k): inputs tile (i, k) at version k, L_kk and 1/d_k; W to tile
+//                 (i, k), L to tile (k, i) (the right-hand side: the W and y
+//                 rows), flag (i, k) = k+1
+//   update (i, j, s): inputs tile (i, j) at version s, W_is, L_js; result to
+//                 tile (i, j) (lower part of a diagonal tile, row 0 of the
+//                 right-hand side), flag (i, j) = s+1
+//   inverse J:    input L_JJ; M_J to its slot, inverse flag J = 1
+//   lookahead (r, s+1, s), right after panel (r, s), r = s+2: step s on
+//                 tiles (r, s+1) and (r, r) with W and L of that panel; the
+//                 two tiles are the chain CTA's inputs for step s+1 and go
+//                 straight into its shared memory (st.async, counted on its
+//                 mbarrier), not to the workspace
+enum : int { kTaskPanel = 0, kTaskUpdate = 1, kTaskInv = 2, kTaskLook = 3 };
 
-__device__ void task_store(const Geo& g, double* ws, int* fl, const double* out, int kind, int i, int j, int s) {
+// Stage layout (doubles): A (16 x 16), then W (or L_kk) and L, padded.
+constexpr int kStA = 0;
+constexpr int kStW = kTile;
+constexpr int kStL = kTile + kPadTile;
+constexpr int kStRd = kTile + kPadTile;  // 1/d of a panel's L_kk (the L slot is free)
+
+// Warp 9: a 16x16 tile (or only its row 0) at version v into shared memory,
+// two elements per load.
+__device__ __forceinline__ void stage_tile(const Geo& g, const double* __restrict__ S, const double* ws, int i, int j,
+                                           int v, double* dst, int stride, bool row0) {
+  const int lane = threadIdx.x & 31;
+  double2 a[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int e = 2 * (lane + 32 * u), rr = e >> 4, cc = e & 15;
+    a[u] = make_double2(0.0, 0.0);
+    if (!row0 || rr == 0) {
+      if (v == 0)
+        a[u] = *reinterpret_cast<const double2*>(S + s_at(g.ld, g.nblk, i, j, rr, cc));
+      else
+        a[u] = __ldcg(reinterpret_cast<const double2*>(ws + w_at(g, i, j, rr, cc)));
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int e = 2 * (lane + 32 * u), rr = e >> 4, cc = e & 15;
+    if (!row0 || rr == 0) {
+      dst[rr * stride + cc] = a[u].x;
+      dst[rr * stride + cc + 1] = a[u].y;
+    }
+  }
+}
+
+// Warp 9: wait for task (kind, i, j, s)'s producers, then stage its inputs.
+__device__ void load_task(const Geo& g, const double* __restrict__ S, const double* ws, int* fl, double* st, int kind,
+                          int i, int j, int s) {
   const int lane = threadIdx.x & 31;
   const int nblk = g.nblk;
+  int* abort_word = fl + g.abort_index();
+  int* f = nullptr;
+  int v = 0;
+  if (kind == kTaskPanel) {  // (i, k = j) at version k, diagonal tile k factored
+    if (lane == 0 && j > 0) f = flag_at(fl, nblk, i, j), v = j;
+    if (lane == 1) f = flag_at(fl, nblk, j, j), v = j + 1;
+  } else if (kind == kTaskUpdate) {  // tile at version s, panels (i, s) and (j, s)
+    if (lane == 0 && s > 0) f = flag_at(fl, nblk, i, j), v = s;
+    if (lane == 1) f = flag_at(fl, nblk, i, s), v = s + 1;
+    if (lane == 2) f = flag_at(fl, nblk, j, s), v = s + 1;
+  } else if (kind == kTaskLook) {  // tiles (i, j = s+1) and (i, i) at version s, the chain's panel (s+1, s)
+    if (lane == 0 && s > 0) f = flag_at(fl, nblk, i, j), v = s;
+    if (lane == 1 && s > 0 && i < nblk) f = flag_at(fl, nblk, i, i), v = s;
+    if (lane == 2) f = flag_at(fl, nblk, j, s), v = s + 1;
+  } else {  // diagonal tile i factored
+    if (lane == 0) f = flag_at(fl, nblk, i, i), v = i + 1;
+  }
+  if (f) wait_ge(f, v, abort_word);
+  __syncwarp();
+  if (kind == kTaskPanel) {
+    stage_tile(g, S, ws, i, j, j, st + kStA, kB, i == nblk);
+    stage_tile(g, S, ws, j, j, 1, st + kStW, kPad, false);
+    if (lane < kB) st[kStRd + lane] = __ldcg(ws + g.rhs_rd() + kB * j + lane);
+  } else if (kind == kTaskUpdate) {
+    stage_tile(g, S, ws, i, j, s, st + kStA, kB, i == nblk);
+    stage_tile(g, S, ws, i, s, 1, st + kStW, kPad, i == nblk);
+    stage_tile(g, S, ws, s, j, 1, st + kStL, kPad, false);  // L_js sits in the upper tile (s, j)
+  } else if (kind == kTaskLook) {
+    stage_tile(g, S, ws, i, j, s, st + kStA, kB, i == nblk);
+    if (i < nblk) stage_tile(g, S, ws, i, i, s, st + kStW, kB, false);
+    stage_tile(g, S, ws, s, j, 1, st + kStL, kPad, false);
+  } else {
+    stage_tile(g, S, ws, i, i, 1, st + kStW, kPad, false);
+  }
+}
+
+// Warps 0-7: the result of a staged task into out (512 doubles); prev is
+// the previous task's result (the panel a lookahead task continues).
+__device__ void math_task(const Geo& g, const double* st, double* out, const double* prev, double* sm, int kind,
+                          int i, int j) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const bool rhs = (i == g.nblk);
+  const double* Lk = st + kStW;
+  if (kind == kTaskLook) {
+    // tile (i, j) -= W L_{j,j-1}^T and tile (i, i) -= W L^T (lower part),
+    // W and L of panel (i, j-1) in prev; L goes to out, padded, first
+    const int rr = tid >> 4, cc = tid & 15;
+    out[rr * kPad + cc] = prev[kTile + tid];
+    bar_sync(kBarMath, kMath);
+    const double* wr = prev + rr * kB;
+    const double* l1 = st + kStL + cc * kPad;
+    const double* l2 = out + cc * kPad;
+    double a0 = 0.0, a1 = 0.0, b0 = 0.0, b1 = 0.0;
+#pragma unroll
+    for (int q = 0; q < kB; q += 2) {
+      a0 = fma(wr[q], l1[q], a0);
+      a1 = fma(wr[q + 1], l1[q + 1], a1);
+      b0 = fma(wr[q], l2[q], b0);
+      b1 = fma(wr[q + 1], l2[q + 1], b1);
+    }
+    // into the chain CTA: P[j & 1] and D[(j+1) & 1], counted on its mbarrier
+    // rx[j & 1]
+    const unsigned rbar = cluster_addr(sm + g.c_rx(j & 1), 0);
+    if (!rhs || rr == 0) st_async(cluster_addr(sm + g.c_p(j & 1) + tid, 0), st[kStA + tid] - (a0 + a1), rbar);
+    if (!rhs)
+      st_async(cluster_addr(sm + g.c_diag((j + 1) & 1) + tid, 0), rr >= cc ? st[kStW + tid] - (b0 + b1) : 0.0, rbar);
+    return;
+  }
+  if (kind == kTaskPanel) {
+    // W = A L_kk^-T (two rows per warp), L = W D_k^-1
+    const int row = 2 * warp + (lane >> 4), c = lane & 15;
+    if (!rhs || warp == 0) {
+      const double a = fwd_rows((!rhs || row == 0) ? st[kStA + row * kB + c] : 0.0, Lk, lane);
+      out[row * kB + c] = a;
+      out[kTile + row * kB + c] = a * st[kStRd + c];
+    }
+  } else if (kind == kTaskUpdate) {
+    // A_ij -= W_is L_js^T (lower part of a diagonal tile, row 0 of the
+    // right-hand side)
+    const int rr = tid >> 4, cc = tid & 15;
+    if (rhs ? rr == 0 : (i != j || rr >= cc)) {
+      const double* wr = st + kStW + rr * kPad;
+      const double* lc = st + kStL + cc * kPad;
+      double s0 = 0.0, s1 = 0.0;
+#pragma unroll
+      for (int q = 0; q < kB; q += 2) {
+        s0 = fma(wr[q], lc[q], s0);
+        s1 = fma(wr[q + 1], lc[q + 1], s1);
+      }
+      out[tid] = st[kStA + tid] - (s0 + s1);
+    }
+  } else {
+    // M_J = L_JJ^-T, the panel solve of the identity, stored transposed
+    // (M_J[c][q] at [q * 16 + c])
+    const int row = 2 * warp + (lane >> 4), c = lane & 15;
+    out[c * kB + row] = fwd_rows(row == c ? 1.0 : 0.0, Lk, lane);
+  }
+}
+
+// Warp 8: store a result, fence it and release its flag.
+__device__ void store_task(const Geo& g, double* ws, int* fl, const double* out, int kind, int i, int j, int s) {
+  const int lane = threadIdx.x & 31;
+  const int nblk = g.nblk;
+  if (kind == kTaskLook) return;  // went to the chain CTA directly
   int* f = nullptr;
   int v = 0;
   if (kind == kTaskPanel) {
     if (i < nblk) {
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int e = lane + 32 * u;
-        __stcg(ws + g.tile_off(i, j) + e, out[e]);
-        __stcg(ws + g.tile_off(j, i) + e, out[kTile + e]);
+      for (int u = 0; u < 4; ++u) {
+        const int e = 2 * (lane + 32 * u);
+        __stcg(reinterpret_cast<double2*>(ws + g.tile_off(i, j) + e), *reinterpret_cast<const double2*>(out + e));
+        __stcg(reinterpret_cast<double2*>(ws + g.tile_off(j, i) + e),
+               *reinterpret_cast<const double2*>(out + kTile + e));
       }
     } else if (lane < kB) {
       __stcg(ws + g.rhs_w() + kB * j + lane, out[lane]);
@@ -590,80 +774,17 @@ __device__ void task_store(const Geo& g, double* ws, int* fl, const double* out,
     v = s + 1;
   } else {
 #pragma unroll
-    for (int u = 0; u < 8; ++u) __stcg(ws + g.m_offset() + (size_t)i * kTile + lane + 32 * u, out[lane + 32 * u]);
+    for (int u = 0; u < 4; ++u) {
+      const int e = 2 * (lane + 32 * u);
+      __stcg(reinterpret_cast<double2*>(ws + g.m_offset() + (size_t)i * kTile + e),
+             *reinterpret_cast<const double2*>(out + e));
+    }
     f = fl + g.inv_index(i);
     v = 1;
   }
   __threadfence();
   __syncwarp();
   if (lane == 0) st_release(f, v);
-}
-
-// Panel tile (i, k), i >= k+2 (i = nblk: the right-hand side), at version k:
-// W = A L_kk^-T, L = W D_k^-1 into out[0..256) and out[256..512).
-__device__ void math_panel(const Geo& g, const double* __restrict__ S, const double* ws, int* fl, double* sm,
-                           double* out, int i, int k) {
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int nblk = g.nblk;
-  int* abort_word = fl + g.abort_index();
-  double* Lk = sm + g.w_lk();
-  math_wait3(k > 0 ? flag_at(fl, nblk, i, k) : nullptr, k, flag_at(fl, nblk, k, k), k + 1, nullptr, 0, abort_word);
-  const bool rhs = (i == nblk);
-  const int row = 2 * warp + (lane >> 4), c = lane & 15;
-  double a = 0.0;
-  if (!rhs || row == 0) a = tile_read(g, S, ws, i, k, row, c, k);
-  Lk[(tid >> 4) * kPad + (tid & 15)] = __ldcg(ws + g.tile_off(k, k) + tid);
-  if (tid < kB) Lk[kPadTile + tid] = __ldcg(ws + g.rhs_rd() + kB * k + tid);
-  bar_sync(kBarMath, kMath);
-  if (!rhs || warp == 0) {
-    a = fwd_rows(a, Lk, lane);
-    out[row * kB + c] = a;
-    out[kTile + row * kB + c] = a * Lk[kPadTile + c];
-  }
-}
-
-// M_J = L_JJ^-T: the panel solve of the identity, stored transposed
-// (M_J[c][q] at [q * 16 + c]).
-__device__ void math_inv(const Geo& g, const double* ws, int* fl, double* sm, double* out, int J) {
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  int* abort_word = fl + g.abort_index();
-  double* Lk = sm + g.w_lk();
-  math_wait3(flag_at(fl, g.nblk, J, J), J + 1, nullptr, 0, nullptr, 0, abort_word);
-  Lk[(tid >> 4) * kPad + (tid & 15)] = __ldcg(ws + g.tile_off(J, J) + tid);
-  bar_sync(kBarMath, kMath);
-  const int row = 2 * warp + (lane >> 4), c = lane & 15;
-  out[c * kB + row] = fwd_rows(row == c ? 1.0 : 0.0, Lk, lane);
-}
-
-// Trailing update of tile (i, j) with step s: A_ij -= W_is L_js^T.
-__device__ void math_update(const Geo& g, const double* __restrict__ S, const double* ws, int* fl, double* sm,
-                            double* out, int i, int j, int s) {
-  const int tid = threadIdx.x;
-  const int nblk = g.nblk;
-  int* abort_word = fl + g.abort_index();
-  double* Wt = sm + g.w_w();
-  double* Lt = sm + g.w_l();
-  math_wait3(s > 0 ? flag_at(fl, nblk, i, j) : nullptr, s, flag_at(fl, nblk, i, s), s + 1, flag_at(fl, nblk, j, s),
-             s + 1, abort_word);
-  const bool rhs = (i == nblk);
-  const int rr = tid >> 4, cc = tid & 15;
-  const bool mine = rhs ? rr == 0 : (i != j || rr >= cc);
-  double a = 0.0;
-  if (mine) a = tile_read(g, S, ws, i, j, rr, cc, s);
-  if (!rhs || rr == 0) Wt[rr * kPad + cc] = __ldcg(ws + w_at(g, i, s, rr, cc));
-  Lt[rr * kPad + cc] = __ldcg(ws + l_at(g, j, s, rr, cc));
-  bar_sync(kBarMath, kMath);
-  if (mine) {
-    const double* wr = Wt + rr * kPad;
-    const double* lc = Lt + cc * kPad;
-    double s0 = 0.0, s1 = 0.0;
-#pragma unroll
-    for (int q = 0; q < kB; q += 2) {
-      s0 = fma(wr[q], lc[q], s0);
-      s1 = fma(wr[q + 1], lc[q + 1], s1);
-    }
-    out[tid] = a - (s0 + s1);
-  }
 }
 
 // The worker's share of a segment of cnt tasks of the global order: task m
@@ -680,20 +801,32 @@ struct Deal {
   }
 };
 
-// Calls f(kind, i, j, s) for this worker's tasks in order.
+// Calls f(kind, i, j, s) for this worker's tasks in order.  Worker 1 runs
+// only the lookahead rows, so it is idle when the chain CTA publishes the
+// diagonal tile they wait for; the other tasks are dealt over workers
+// 2..C-1.
 template <typename F>
 __device__ void worker_tasks(const Geo& g, int rank, F&& f) {
   const int nblk = g.nblk;
-  Deal d{g.C - 1, rank - 1, 0};
+  if (rank == 1) {
+    // (0) block row k+2, the chain CTA's next input: its panel, then step k
+    //     on its tiles (k+2, k+1) and (k+2, k+2)
+    for (int k = 0; k + 2 <= nblk; ++k) {
+      f(kTaskPanel, k + 2, k, k);
+      f(kTaskLook, k + 2, k + 1, k);
+    }
+    return;
+  }
+  Deal d{g.C - 2, rank - 2, 0};
   for (int k = 0; k < nblk; ++k) {
-    // (1) panels (i, k), i >= k+2, right-hand side last (the last column's
-    //     right-hand-side panel is the chain CTA's)
-    if (k + 1 < nblk) d.segment(nblk - k - 1, [&](int idx) { f(kTaskPanel, k + 2 + idx, k, k); });
-    // (2) step k on block column k+1 below its diagonal tile (the chain CTA
-    //     updates the diagonal tile itself)
-    if (k + 1 < nblk) d.segment(nblk - k - 1, [&](int idx) { f(kTaskUpdate, k + 2 + idx, k + 1, k); });
-    // (3) step k on block column k+2, diagonal tile included
-    if (k + 2 < nblk) d.segment(nblk - k - 1, [&](int idx) { f(kTaskUpdate, k + 2 + idx, k + 2, k); });
+    // (1) the other panels (i, k), i >= k+3, right-hand side last (the last
+    //     column's right-hand-side panel is the chain CTA's)
+    if (k + 1 < nblk) d.segment(nblk - k - 2, [&](int idx) { f(kTaskPanel, k + 3 + idx, k, k); });
+    // (2) step k on block column k+1 below (the chain CTA updates the
+    //     diagonal tile itself)
+    if (k + 1 < nblk) d.segment(nblk - k - 2, [&](int idx) { f(kTaskUpdate, k + 3 + idx, k + 1, k); });
+    // (3) step k on block column k+2 below
+    if (k + 2 < nblk) d.segment(nblk - k - 2, [&](int idx) { f(kTaskUpdate, k + 3 + idx, k + 2, k); });
     // (4b) the deferred bulk of step k-1: block columns k+3 .. nblk-1
     if (k >= 1 && k + 3 < nblk) {
       int cnt = 0;
@@ -716,31 +849,36 @@ __device__ void worker_tasks(const Geo& g, int rank, F&& f) {
 
 __device__ void worker_cta(const Geo& g, const double* __restrict__ S, double* ws, int* fl, double* sm, int rank) {
   const int warp = threadIdx.x >> 5;
-  int n = 0;  // tasks run so far; result buffer n & 1
+  int n = 0;  // tasks so far; stage and result buffer n & 1
   if (warp < 8) {
     worker_tasks(g, rank, [&](int kind, int i, int j, int s) {
       const int b = n & 1;
-      double* out = sm + g.w_out(b);
-      if (n >= 2) bar_sync(kBarOutFree + b, kThreads);  // warp 8 has stored task n-2
-      if (kind == kTaskPanel)
-        math_panel(g, S, ws, fl, sm, out, i, j);
-      else if (kind == kTaskUpdate)
-        math_update(g, S, ws, fl, sm, out, i, j, s);
-      else
-        math_inv(g, ws, fl, sm, out, i);
-      bar_arrive(kBarOutFull + b, kThreads);
+      bar_sync(kBarInFull + b, kPair);                   // warp 9 has staged task n
+      if (n >= 2) bar_sync(kBarOutFree + b, kPair);      // warp 8 has stored task n-2
+      math_task(g, sm + g.w_stage(b), sm + g.w_out(b), sm + g.w_out(b ^ 1), sm, kind, i, j);
+      bar_arrive(kBarInFree + b, kPair);
+      bar_arrive(kBarOutFull + b, kPair);
       ++n;
     });
     // balance warp 8's last two releases
-    for (int q = max(n - 2, 0); q < n; ++q) bar_sync(kBarOutFree + (q & 1), kThreads);
+    for (int q = max(n - 2, 0); q < n; ++q) bar_sync(kBarOutFree + (q & 1), kPair);
+  } else if (warp == 8) {
+    worker_tasks(g, rank, [&](int kind, int i, int j, int s) {
+      const int b = n & 1;
+      bar_sync(kBarOutFull + b, kPair);
+      store_task(g, ws, fl, sm + g.w_out(b), kind, i, j, s);
+      bar_arrive(kBarOutFree + b, kPair);
+      ++n;
+    });
   } else {
     worker_tasks(g, rank, [&](int kind, int i, int j, int s) {
       const int b = n & 1;
-      bar_sync(kBarOutFull + b, kThreads);
-      task_store(g, ws, fl, sm + g.w_out(b), kind, i, j, s);
-      bar_arrive(kBarOutFree + b, kThreads);
+      if (n >= 2) bar_sync(kBarInFree + b, kPair);  // warps 0-7 are done with task n-2's stage
+      load_task(g, S, ws, fl, sm + g.w_stage(b), kind, i, j, s);
+      bar_arrive(kBarInFull + b, kPair);
       ++n;
     });
+    for (int q = max(n - 2, 0); q < n; ++q) bar_sync(kBarInFree + (q & 1), kPair);
   }
 }
 
@@ -750,6 +888,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_ldlt_cluster(const double* __re
   cg::cluster_group cl = cg::this_cluster();
   const int r = (int)cl.block_rank();
   int* fl = reinterpret_cast<int*>(ws + g.flag_offset());
+  // the chain CTA's receive mbarriers are ready before any worker can push
+  if (r == 0 && threadIdx.x == kMath) {
+    mbar_init(reinterpret_cast<uint64_t*>(sm + g.c_rx(0)), 1);
+    mbar_init(reinterpret_cast<uint64_t*>(sm + g.c_rx(1)), 1);
+    fence_mbar_init();
+  }
   // the version flags and the abort word start at zero in every launch
   for (int e = r * kThreads + (int)threadIdx.x; e < g.flag_count(); e += g.C * kThreads) fl[e] = 0;
   __threadfence();
