@@ -25,11 +25,10 @@
 //     arrive/sync barriers and never wait for its stores or fences.
 //   * CTAs 1..C-1 (workers) run every other task in one fixed global order,
 //     dealt round robin: panel solves (i, k) for i >= k+3 and the right-hand
-//     side, the trailing updates A_ij -= W_ik L_jk^T, and the inverses
-//     M_J = L_JJ^-T for the backward solve.  The order is the right-looking
+//     side, and the trailing updates A_ij -= W_ik L_jk^T.  The order is the right-looking
 //     schedule with lookahead: per step k, the panels, then the updates of
 //     block columns k+1 and k+2, then the deferred bulk of step k-1, then
-//     block column k+3 of step k, then the inverse of diagonal tile k-1.
+//     block column k+3 of step k.
 //     Every task's inputs come earlier in that order (or from the chain
 //     CTA's step k), so waiting on them in order cannot deadlock.  A
 //     worker's warps 8 and 9 store each result (fence, flag) and stage the
@@ -37,7 +36,8 @@
 //   * Worker 1 runs only block row k+2 of each step k: its panel, then the
 //     updates of its tiles (k+2, k+1) and (k+2, k+2), which it pushes
 //     straight into the chain CTA's shared memory (st.async, counted on an
-//     mbarrier there) as the chain CTA's inputs for step k+1.
+//     mbarrier there) as the chain CTA's inputs for step k+1; then the
+//     inverse M_k of diagonal tile k.
 //   * The workspace is tile-major: 16x16 tiles of 2 KB, lower positions for
 //     the working tiles (A, then W = L D after its panel solve), upper
 //     positions (j, i) for L_ij.  Each tile has a version flag: the number of
@@ -810,10 +810,12 @@ __device__ void worker_tasks(const Geo& g, int rank, F&& f) {
   const int nblk = g.nblk;
   if (rank == 1) {
     // (0) block row k+2, the chain CTA's next input: its panel, then step k
-    //     on its tiles (k+2, k+1) and (k+2, k+2)
+    //     on its tiles (k+2, k+1) and (k+2, k+2); then, while the chain CTA
+    //     factors tile k+1, the backward-solve inverse of diagonal tile k
     for (int k = 0; k + 2 <= nblk; ++k) {
       f(kTaskPanel, k + 2, k, k);
       f(kTaskLook, k + 2, k + 1, k);
+      f(kTaskInv, k, k, 0);
     }
     return;
   }
@@ -842,8 +844,6 @@ __device__ void worker_tasks(const Geo& g, int rank, F&& f) {
     }
     // (4a) step k on block column k+3
     if (k + 3 < nblk) d.segment(nblk - k - 2, [&](int idx) { f(kTaskUpdate, k + 3 + idx, k + 3, k); });
-    // (5) the backward-solve inverse of diagonal tile k-1
-    if (k >= 1) d.segment(1, [&](int) { f(kTaskInv, k - 1, k - 1, 0); });
   }
 }
 
