@@ -391,12 +391,26 @@ __global__ void k_block_ids(int Kf, const int* flag_scan, const int* present, in
   }
 }
 
-// pair counts per block: each thread counts its point's pairs per block in
-// a short local list first (a point has few distinct pose pairs), so the
-// global atomics are one per (point, block)
-__global__ void k_pair_block_count(int Lf, int Kf, const int* pt_begin, const int* cph, const int* blk_of,
+// pair counts per block.  When the block counters fit in shared memory each
+// CTA counts its points' pairs there and adds one total per block it saw to
+// the global counters; otherwise each thread counts its point's pairs per
+// block in a short local list first (a point has few distinct pose pairs),
+// so the global atomics are one per (point, block).
+constexpr int kBlockHistMax = 12288;  // 48 KB of int counters
+__global__ void k_pair_block_count(int Lf, int Kf, int nblk, const int* pt_begin, const int* cph, const int* blk_of,
                                    int* bcnt) {
+  extern __shared__ int hist[];
   const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (nblk <= kBlockHistMax) {
+    for (int k = threadIdx.x; k < nblk; k += blockDim.x) hist[k] = 0;
+    __syncthreads();
+    if (l < Lf)
+      visit_pairs(pt_begin[l], pt_begin[l + 1], cph, [&](int a, int b, int, int) { atomicAdd(&hist[blk_of[a * Kf + b]], 1); });
+    __syncthreads();
+    for (int k = threadIdx.x; k < nblk; k += blockDim.x)
+      if (hist[k]) atomicAdd(&bcnt[k], hist[k]);
+    return;
+  }
   if (l >= Lf) return;
   constexpr int kList = 8;
   int key[kList] = {0}, cnt[kList] = {0}, n = 0;
@@ -702,7 +716,11 @@ int compiler_phase1(DeviceCompiler* c, const HostProblem& hp, cudaStream_t st, S
   CK(c->bcb.ensure(nblk + 1));
   CK(cudaMemsetAsync(c->bcnt.p, 0, (nblk + 1) * sizeof(int), st));
   if (KK) k_block_ids<<<blocks((int)KK), 256, 0, st>>>(Kf, c->blk_id.p, c->present.p, c->blk_of.p, c->block_ab.p);
-  if (Lf) k_pair_block_count<<<blocks(Lf, 128), 128, 0, st>>>(Lf, Kf, c->pt_begin.p, c->cph.p, c->blk_of.p, c->bcnt.p);
+  if (Lf) {
+    const size_t hist = nblk <= kBlockHistMax ? (size_t)nblk * sizeof(int) : 0;
+    k_pair_block_count<<<blocks(Lf, 256), 256, hist, st>>>(Lf, Kf, nblk, c->pt_begin.p, c->cph.p, c->blk_of.p,
+                                                            c->bcnt.p);
+  }
   if (nblk) k_pchunk_count<<<blocks(nblk), 256, 0, st>>>(nblk, c->bcnt.p, c->bcb.p);
   if ((rc = c->scan(c->bcb.p, nblk, st, err))) return rc;   // block_chunk_begin; npc at [nblk]
   if ((rc = c->scan(c->bcnt.p, nblk, st, err))) return rc;  // pair offset of each block
