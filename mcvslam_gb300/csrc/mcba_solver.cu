@@ -297,6 +297,22 @@ __global__ void __launch_bounds__(kLinThreads) k_linearize(Bufs B) {
   }
 }
 
+// a += p[c0 * stride] + .. + p[(c1 - 1) * stride], in that order; the loads
+// go out eight at a time, so a long range costs a few L2 round trips, not
+// one per term.
+template <typename R>
+__device__ __forceinline__ void acc_range(Acc<R>& a, const Acc<R>* p, int c0, int c1, size_t stride) {
+  int c = c0;
+  for (; c + 8 <= c1; c += 8) {
+    Acc<R> v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = p[(size_t)(c + u) * stride];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) a.add(v[u]);
+  }
+  for (; c < c1; ++c) a.add(p[(size_t)c * stride]);
+}
+
 // Hpp / b_p: sum of the chunk partials of each free pose (warp per pose),
 // stored in FP64.
 template <typename R>
@@ -306,7 +322,7 @@ __device__ __forceinline__ void pose_reduce_warp(const Bufs& B, int Kf, int i, i
   const Acc<R>* part = reinterpret_cast<const Acc<R>*>(B.partials);
   Acc<R> a;
   a.zero();
-  for (int c = c0; c < c1; ++c) a.add(part[(size_t)c * 32 + lane]);
+  acc_range(a, part + lane, c0, c1, 32);
   const double s = a.value();
   double* H = B.Hpp + (size_t)i * 36;
   if (lane < 21) {
@@ -331,6 +347,7 @@ __device__ __forceinline__ void point_reduce_thread(const Bufs& B, int Lf, int l
   R s[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) s[k] = R(0);
+#pragma unroll 4
   for (int e = e0; e < e1; ++e) {
     const R* row = Ptrs<R>::p(B.rows) + (size_t)e * kRow + 18;
 #pragma unroll
@@ -534,7 +551,7 @@ __global__ void k_schur_assemble(Bufs B, int ld) {
   const Acc<R>* part = reinterpret_cast<const Acc<R>*>(B.ppart);
   Acc<R> v;
   v.zero();
-  for (int c = c0; c < c1; ++c) v.add(part[(size_t)c * 36 + t]);
+  acc_range(v, part + t, c0, c1, 36);
   const int r = t / 6, q = t % 6;
   if (a == bb) {
     double d = B.Hpp[(size_t)a * 36 + t] - v.value();
@@ -545,7 +562,7 @@ __global__ void k_schur_assemble(Bufs B, int ld) {
       const Acc<R>* qp = reinterpret_cast<const Acc<R>*>(B.qpart);
       Acc<R> qs;
       qs.zero();
-      for (int ch = B.pose_chunk_begin[a]; ch < B.pose_chunk_begin[a + 1]; ++ch) qs.add(qp[(size_t)ch * 6 + t]);
+      acc_range(qs, qp + t, B.pose_chunk_begin[a], B.pose_chunk_begin[a + 1], 6);
       B.S[(size_t)ld * ld + 6 * a + t] = B.bp[6 * (size_t)a + t] - qs.value();
     }
   } else {
@@ -692,6 +709,7 @@ __device__ __forceinline__ void backsub_block(const Bufs& B, int Lf, int n, int 
     const R* bl = Ptrs<R>::p(B.bl) + 3 * (size_t)l;
     if (B.lm->solve_ok) {
       R cl[3] = {bl[0], bl[1], bl[2]};
+#pragma unroll 4
       for (int e = B.pt_begin[l]; e < B.pt_begin[l + 1]; ++e) {
         const int ph = B.canon_pose_h[e];
         if (ph < 0) continue;
