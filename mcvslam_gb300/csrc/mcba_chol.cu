@@ -937,7 +937,12 @@ int chol_cluster_plan(int ld, int n, CholPlan* plan) {
   // least three
   int R = nblk;
   while (R > std::min(nblk, 3) && make_geo(16, ld, n, R).total() * sizeof(double) + reserve > (size_t)max_smem) --R;
-  for (int C : {16, 8}) {
+  // cluster size by the work: a chain CTA, the lookahead worker and enough
+  // general workers for the trailing updates (small systems, e.g. the
+  // windows of a batch that run side by side, take fewer SMs)
+  const int Cpref = nblk >= 10 ? 16 : (nblk >= 5 ? 8 : 4);
+  for (int C : {16, 8, 4}) {
+    if (C > Cpref) continue;
     const Geo g = make_geo(C, ld, n, R);
     const size_t bytes = g.total() * sizeof(double);
     if (bytes + reserve > (size_t)max_smem) continue;

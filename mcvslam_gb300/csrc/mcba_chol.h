@@ -14,7 +14,7 @@ struct CholPlan {
   size_t smem_bytes = 0;
 };
 
-// Chooses a cluster size (16, else 8) for the n x n system (row stride ld)
+// Chooses a cluster size (16, 8 or 4 CTAs by the size) for the n x n system (row stride ld)
 // and the number of backward-solve rows staged in shared memory; returns 0
 // (plan.ok = false) when the system is too large for the cluster solve.
 int chol_cluster_plan(int ld, int n, CholPlan* plan);
