@@ -280,6 +280,20 @@ def test_indefinite_reduced_system_follows_oracle(precision, gpu):
         compare_logs(log, o["log"])
 
 
+@pytest.mark.parametrize("n_kf", [42, 66])
+def test_cluster_solve_up_to_its_largest_size_follows_oracle(n_kf, gpu):
+    # 40 and 64 free keyframes: reduced systems of 240 and 384 unknowns (15 and
+    # 24 tile rows, the largest the cluster factorisation takes), where the
+    # backward solve holds only part of the rows in shared memory at a time;
+    # corridor layout, so the reduced matrix has absent blocks
+    pr = synth.local_ba(n_kf, n_kf * 60, seed=78, corridor=True)
+    o = oracle.optimize(pr, 5)
+    g = ba.solve(pr, 5, "fp64")
+    assert g["stats"]["iterations"] == o["ret"]
+    compare_logs(g["log"], o["log"])
+    compare_state(g, o, pr)
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_large_corridor_window_uses_tiled_solve_and_follows_oracle(precision, gpu):
     # 70 free keyframes (reduced system 420 > 384: the tiled factorisation),
