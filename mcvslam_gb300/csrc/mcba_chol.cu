@@ -50,9 +50,15 @@
 //     (one per tile), and per block row only two 16x16 products lie on the
 //     dependency chain (u = t_J - L_{J+1,J}^T x_{J+1}, x_J = M_J u).
 //
-// Every wait has an iteration limit; a CTA that runs out sets an abort word
-// that ends all other waits at once, and the solve then reports failure
-// (*solve_ok = 0) instead of hanging.  A pivot <= 0 clears *solve_ok; the
+// Every wait has a time limit (%globaltimer); a wait that runs out sets an
+// abort word, and the solve then reports failure (*solve_ok = 0) instead of
+// hanging.  Waits on the workers' flags end at once when the abort word is
+// set.  The waits that guard shared memory (the pushes into the chain CTA,
+// the chain CTA's own bulk copies, and the lookahead worker's wait for the
+// chain CTA's panel, which orders its pushes after the chain CTA's
+// mbarrier arms) run to completion even then: their producers run whatever
+// the other flags say, so no copy into shared memory is in flight when a CTA
+// leaves.  A pivot <= 0 clears *solve_ok; the
 // chain CTA, which factors every diagonal tile, then leaves x untouched.  No
 // CTA reads another CTA's shared memory.
 
@@ -77,7 +83,9 @@ constexpr int kTile = kB * kB;
 constexpr int kPad = kB + 1;  // row stride of staged tiles (conflict-free column reads)
 constexpr int kPadTile = kB * kPad;
 constexpr int kMaxBlk = 24;                // block rows handled by the cluster solve (n <= 384)
-constexpr unsigned kSpinLimit = 1u << 21;  // polls per wait (~1 s) before the solve gives up
+constexpr unsigned long long kWaitNs = 1000000000ull;        // a wait on a worker's flag gives up after 1 s
+constexpr unsigned long long kGuardWaitNs = 4000000000ull;   // the waits that guard shared memory, 4 s
+constexpr unsigned kPollCap = 1u << 27;                      // polls per wait, should the timer stall
 
 // named barriers (0 is __syncthreads)
 constexpr int kBarPivot = 1;    // pivot chain and pivot application (160 threads)
@@ -182,37 +190,75 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
   return ok != 0;
 }
 
-// Bounded wait for *p >= v (one thread).  Returns false when this wait ran
-// out (it then sets the abort word) or another CTA already gave up.
-__device__ bool wait_ge(const int* p, int v, int* abort_word) {
-  for (unsigned it = 0; it < kSpinLimit; ++it) {
+__device__ __forceinline__ unsigned long long now_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait for *p >= v (one thread).  Returns false when the wait ran
+// out (it then sets the abort word) or, unless guard, when another wait
+// already ran out.  guard: the flag's producer runs whatever the abort word
+// says, and the wait keeps waiting for it (up to kGuardWaitNs).  The abort
+// word and the timer are read after the first failed poll and then once per
+// 64 polls; the read after the first failed poll also spaces the polls (with
+// back-to-back polls the factorisation measured 3% slower).
+__device__ bool wait_ge(const int* p, int v, int* abort_word, bool guard = false) {
+  unsigned long long t0 = 0;
+  for (unsigned it = 0; it < kPollCap; ++it) {
     if (ld_acquire(p) >= v) return true;
-    if ((it & 63u) == 0 && ld_acquire(abort_word) != 0) return false;
+    if ((it & 63u) == 0) {
+      if (!guard && ld_acquire(abort_word) != 0) return false;
+      const unsigned long long t = now_ns();
+      if (it == 0)
+        t0 = t;
+      else if (t - t0 > (guard ? kGuardWaitNs : kWaitNs))
+        break;
+    }
     if (it > 32) __nanosleep(64);
   }
   atomicExch(abort_word, 1);
   return false;
 }
 
-// Bounded wait for an mbarrier phase; gives up like wait_ge.
+// Bounded wait for an mbarrier phase that only this CTA's own bulk copies
+// complete: copies always land, so it waits whatever the abort word says.
 __device__ void mbar_wait(uint64_t* bar, unsigned parity, int* abort_word) {
-  for (unsigned it = 0; it < kSpinLimit; ++it) {
+  unsigned long long t0 = 0;
+  for (unsigned it = 0; it < kPollCap; ++it) {
     if (mbar_try_wait(bar, parity)) return;
-    if ((it & 63u) == 0 && ld_acquire(abort_word) != 0) return;
+    if ((it & 63u) == 0) {
+      const unsigned long long t = now_ns();
+      if (it == 0)
+        t0 = t;
+      else if (t - t0 > kGuardWaitNs)
+        break;
+    }
   }
   atomicExch(abort_word, 1);
 }
 
+// The same for the phase the lookahead worker's pushes complete; that worker
+// runs every push whatever the abort word says.
 __device__ void mbar_wait_cluster(uint64_t* bar, unsigned parity, int* abort_word) {
-  for (unsigned it = 0; it < kSpinLimit; ++it) {
+  unsigned long long t0 = 0;
+  for (unsigned it = 0; it < kPollCap; ++it) {
     if (mbar_try_wait_cluster(bar, parity)) return;
-    if ((it & 63u) == 0 && ld_acquire(abort_word) != 0) return;
+    if ((it & 63u) == 0) {
+      const unsigned long long t = now_ns();
+      if (it == 0)
+        t0 = t;
+      else if (t - t0 > kGuardWaitNs)
+        break;
+    }
   }
   atomicExch(abort_word, 1);
 }
 
 struct Geo {
   int C, nblk, ld, n, R;  // R: backward-solve row slots in shared memory
+  int hold;               // a flag the workers leave unreleased (-1 in every solve; the test of the
+                          // bounded waits sets it so that a wait runs out)
   // workspace (doubles): nblk x nblk tiles of 256, then the right-hand-side
   // rows W, 1/d and y (16 nblk each), then (as ints) the version flags
   // ((nblk + 1) x nblk), one flag per inverse M_J and the abort word, then
@@ -642,6 +688,7 @@ __device__ void load_task(const Geo& g, const double* __restrict__ S, const doub
   int* abort_word = fl + g.abort_index();
   int* f = nullptr;
   int v = 0;
+  bool guard = false;
   if (kind == kTaskPanel) {  // (i, k = j) at version k, diagonal tile k factored
     if (lane == 0 && j > 0) f = flag_at(fl, nblk, i, j), v = j;
     if (lane == 1) f = flag_at(fl, nblk, j, j), v = j + 1;
@@ -652,11 +699,13 @@ __device__ void load_task(const Geo& g, const double* __restrict__ S, const doub
   } else if (kind == kTaskLook) {  // tiles (i, j = s+1) and (i, i) at version s, the chain's panel (s+1, s)
     if (lane == 0 && s > 0) f = flag_at(fl, nblk, i, j), v = s;
     if (lane == 1 && s > 0 && i < nblk) f = flag_at(fl, nblk, i, i), v = s;
-    if (lane == 2) f = flag_at(fl, nblk, j, s), v = s + 1;
+    // the chain CTA releases its panel after arming the mbarrier the pushes
+    // count on and after its last read of the buffers they overwrite
+    if (lane == 2) f = flag_at(fl, nblk, j, s), v = s + 1, guard = true;
   } else {  // diagonal tile i factored
     if (lane == 0) f = flag_at(fl, nblk, i, i), v = i + 1;
   }
-  if (f) wait_ge(f, v, abort_word);
+  if (f) wait_ge(f, v, abort_word, guard);
   __syncwarp();
   if (kind == kTaskPanel) {
     stage_tile(g, S, ws, i, j, j, st + kStA, kB, i == nblk);
@@ -784,7 +833,7 @@ __device__ void store_task(const Geo& g, double* ws, int* fl, const double* out,
   }
   __threadfence();
   __syncwarp();
-  if (lane == 0) st_release(f, v);
+  if (lane == 0 && (int)(f - fl) != g.hold) st_release(f, v);
 }
 
 // The worker's share of a segment of cnt tasks of the global order: task m
@@ -911,6 +960,7 @@ Geo make_geo(int C, int ld, int n, int R) {
   g.ld = ld;
   g.n = n;
   g.R = R;
+  g.hold = -1;
   return g;
 }
 
