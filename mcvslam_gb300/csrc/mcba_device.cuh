@@ -131,30 +131,35 @@ __device__ __forceinline__ void se3_exp_left(const double* u, const double* qt_i
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j) O2[3 * i + j] = O[3 * i] * O[j] + O[3 * i + 1] * O[3 + j] + O[3 * i + 2] * O[6 + j];
-  double a, b, vb, vc;
-  if (th2 < 1e-10) {  // theta < 1e-5
-    a = 1.0;
-    b = 0.5;
+  double vb, vc, qe[4];
+  if (th2 < 1e-10) {  // theta < 1e-5: R = I + Omega + Omega^2 / 2, then Quaternion(R)
     vb = 0.5;
     vc = 1.0 / 6.0;
+    double R[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) R[i] = ((i % 4 == 0) ? 1.0 : 0.0) + O[i] + 0.5 * O2[i];
+    R_to_quat(R, qe);
   } else {
+    // The quaternion of the Rodrigues rotation R = I + sin(t)/t Omega +
+    // (1 - cos(t))/t^2 Omega^2 is (sin(t/2) w/t, cos(t/2)), which is what
+    // Quaternion(R) returns for it up to rounding, without R's square root
+    // and normalisation on the dependency chain.  V takes sin(t) =
+    // 2 sin(t/2) cos(t/2) and 1 - cos(t) = 2 sin^2(t/2).
     const double inv = rsqrt_newton(th2), theta = th2 * inv;
-    double s, c;
-    sincos(theta, &s, &c);
-    a = s * inv;
-    b = (1 - c) * (inv * inv);
-    vb = b;
+    double sh, ch;
+    sincos(0.5 * theta, &sh, &ch);
+    const double k = sh * inv;
+    qe[0] = w0 * k;
+    qe[1] = w1 * k;
+    qe[2] = w2 * k;
+    qe[3] = ch;
+    const double s = 2.0 * sh * ch;
+    vb = 2.0 * sh * sh * (inv * inv);
     vc = (theta - s) * (inv * inv * inv);
   }
-  double R[9], V[9];
+  double V[9];
 #pragma unroll
-  for (int i = 0; i < 9; ++i) {
-    const double I = (i % 4 == 0) ? 1.0 : 0.0;
-    R[i] = I + a * O[i] + b * O2[i];
-    V[i] = I + vb * O[i] + vc * O2[i];
-  }
-  double qe[4];
-  R_to_quat(R, qe);
+  for (int i = 0; i < 9; ++i) V[i] = ((i % 4 == 0) ? 1.0 : 0.0) + vb * O[i] + vc * O2[i];
   const double te[3] = {V[0] * u[3] + V[1] * u[4] + V[2] * u[5], V[3] * u[3] + V[4] * u[4] + V[5] * u[5],
                         V[6] * u[3] + V[7] * u[4] + V[8] * u[5]};
   // exp(u) * T

@@ -698,51 +698,65 @@ __global__ void __launch_bounds__(256) k_chol_backsolve(const double* S, const d
 
 // Landmark back-substitution (block_solver.hpp:420-446) and point update,
 // plus the point part of computeScale (optimization_algorithm_levenberg.cpp:159-165).
+// Four lanes per point: lane s of the group walks edges s, s+4, .. of the
+// point (so the dependent index -> row/x loads of a point's edges are in
+// flight together), the four partial sums meet in a fixed shuffle tree, and
+// lanes 0-2 then update one coordinate each.
+constexpr int kPtLanes = 4;
+constexpr int kPtsPerBlock = 128 / kPtLanes;  // k_update runs 128-thread blocks
+
 template <typename R>
 __device__ __forceinline__ void backsub_block(const Bufs& B, int Lf, int n, int blk, double* sh) {
-  const int l = blk * blockDim.x + threadIdx.x;
+  const int l = blk * kPtsPerBlock + (int)(threadIdx.x / kPtLanes);
+  const int sub = threadIdx.x % kPtLanes;
   const int cur = B.lm->cur, cand = cur ^ 1;
   const double lam = B.lm->lambda;
+  const bool ok = B.lm->solve_ok != 0;
   double sc = 0.0;
-  if (l < Lf) {
-    double* xl = B.x + n + 3 * (size_t)l;
-    const R* bl = Ptrs<R>::p(B.bl) + 3 * (size_t)l;
-    if (B.lm->solve_ok) {
-      R cl[3] = {bl[0], bl[1], bl[2]};
-#pragma unroll 4
-      for (int e = B.pt_begin[l]; e < B.pt_begin[l + 1]; ++e) {
-        const int ph = B.canon_pose_h[e];
-        if (ph < 0) continue;
-        const R* H = Ptrs<R>::p(B.rows) + (size_t)e * kRow;
-        const double* xp = B.x + 6 * (size_t)ph;
-        R xr[6];
+  R t[3] = {R(0), R(0), R(0)};
+  if (l < Lf && ok) {
+    const int e1 = B.pt_begin[l + 1];
+#pragma unroll 2
+    for (int e = B.pt_begin[l] + sub; e < e1; e += kPtLanes) {
+      const int ph = B.canon_pose_h[e];
+      if (ph < 0) continue;
+      const R* H = Ptrs<R>::p(B.rows) + (size_t)e * kRow;
+      const double* xp = B.x + 6 * (size_t)ph;
+      R xr[6];
 #pragma unroll
-        for (int k = 0; k < 6; ++k) xr[k] = (R)xp[k];
+      for (int k = 0; k < 6; ++k) xr[k] = (R)xp[k];
 #pragma unroll
-        for (int q = 0; q < 3; ++q) {
-          R t = R(0);
+      for (int q = 0; q < 3; ++q) {
+        R u = R(0);
 #pragma unroll
-          for (int k = 0; k < 6; ++k) t += H[k * 3 + q] * xr[k];
-          cl[q] -= t;
-        }
+        for (int k = 0; k < 6; ++k) u += H[k * 3 + q] * xr[k];
+        t[q] += u;
       }
+    }
+  }
+  // the four lanes of a point are adjacent: partial sums meet as (0+1)+(2+3)
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    t[q] += __shfl_xor_sync(0xffffffffu, t[q], 1);
+    t[q] += __shfl_xor_sync(0xffffffffu, t[q], 2);
+  }
+  if (l < Lf && sub < 3) {
+    const int q = sub;
+    const R* bl = Ptrs<R>::p(B.bl) + 3 * (size_t)l;
+    double* xl = B.x + n + 3 * (size_t)l;
+    if (ok) {
+      const R cl[3] = {bl[0] - t[0], bl[1] - t[1], bl[2] - t[2]};
       R Di[9];
       damped_inverse<R>(Ptrs<R>::p(B.Hll) + (size_t)l * 6, (R)lam, Di);
-#pragma unroll
-      for (int q = 0; q < 3; ++q) xl[q] = (double)(Di[3 * q] * cl[0] + Di[3 * q + 1] * cl[1] + Di[3 * q + 2] * cl[2]);
+      xl[q] = (double)(Di[3 * q] * cl[0] + Di[3 * q + 1] * cl[1] + Di[3 * q + 2] * cl[2]);
     }
     const int id = B.free_point_ids[l];
-    const double* X0 = B.Xd[cur] + 3 * (size_t)id;
-    double* X1 = B.Xd[cand] + 3 * (size_t)id;
-    double nx[3];
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-      const double d = xl[q];
-      nx[q] = X0[q] + d;
-      X1[q] = nx[q];
-      sc += d * (lam * d + (double)bl[q]);
-    }
-    B.Xf[cand][id] = make_float4((float)nx[0], (float)nx[1], (float)nx[2], 0.f);
+    const double d = xl[q];
+    const double nx = B.Xd[cur][3 * (size_t)id + q] + d;
+    B.Xd[cand][3 * (size_t)id + q] = nx;
+    sc = d * (lam * d + (double)bl[q]);
+    reinterpret_cast<float*>(B.Xf[cand] + id)[q] = (float)nx;
+    if (q == 0) reinterpret_cast<float*>(B.Xf[cand] + id)[3] = 0.f;
   }
   const double tot = block_sum(sc, sh);
   if (threadIdx.x == 0) B.scale_part[blk] = tot;
@@ -801,23 +815,35 @@ __global__ void k_update(Bufs B, int Lf, int n, int Kf, int npose_blocks, int np
 }
 
 // activeRobustChi2 (sparse_optimizer.cpp:102-116) at the current (which = 0)
-// or candidate (which = 1) state: one partial per CTA.
+// or candidate (which = 1) state: one partial per CTA.  FP32 edges are
+// summed per warp as float-float pairs (TwoSum, ~48-bit significand), so
+// the FP64 pipe, which is slow on this part, sees only the eight warp sums.
 template <typename R>
 __global__ void __launch_bounds__(256) k_cost(Bufs B, int E, int which) {
   __shared__ double sh[32];
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const StateView v = make_view(B, B.lm->cur ^ which);
-  double rho = 0.0;
+  R rho = R(0);
   if (j < E) {
     const EdgeRec r = B.recs[j];
     const float obs[3] = {B.obs[3 * (size_t)j], B.obs[3 * (size_t)j + 1], B.obs[3 * (size_t)j + 2]};
     R Pb[3], Pc[3], e[3], chi2;
     transform(r, v, Pb, Pc);
     edge_error<R>(r, obs, v, Pc, e, chi2);
-    rho = r.robust ? (double)huber_rho<R>(chi2, (R)r.delta) : (double)chi2;
+    rho = r.robust ? huber_rho<R>(chi2, (R)r.delta) : chi2;
   }
-  const double tot = block_sum(rho, sh);
-  if (threadIdx.x == 0) B.cost_part[blockIdx.x] = tot;
+  Acc<R> a;
+  a.zero();
+  a.add(rho);
+  a = warp_sum_acc(a);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) sh[wid] = a.value();
+  __syncthreads();
+  if (wid == 0) {
+    double t = (lane < nw) ? sh[lane] : 0.0;
+    t = warp_sum(t);
+    if (lane == 0) B.cost_part[blockIdx.x] = t;
+  }
 }
 
 __device__ double sum_partials(const double* p, int n, double* sh) {
@@ -836,13 +862,39 @@ __global__ void k_lm_begin(Bufs B, int ncost) {
 }
 
 // One LM trial's decision (optimization_algorithm_levenberg.cpp:113-141).
+// The two partial sums run side by side (each in the order and tree of
+// sum_partials), and thread 0 works on a register copy of the LM state,
+// loaded before the sums and stored once at the end, so the decision is
+// not a chain of dependent global loads.
 __global__ void k_lm_decide(Bufs B, int ncost, int nscale, cudaGraphConditionalHandle h_trial, int in_graph) {
-  __shared__ double sh[32];
-  const double tempChi0 = sum_partials(B.cost_part, ncost, sh);
+  __shared__ double sh[64];
+  LMState st;
+  if (threadIdx.x == 0) st = *B.lm;
+  double c = 0.0, d = 0.0;
+  for (int i = threadIdx.x; i < ncost; i += blockDim.x) c += B.cost_part[i];
+  for (int i = threadIdx.x; i < nscale; i += blockDim.x) d += B.scale_part[i];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    c += __shfl_xor_sync(0xffffffffu, c, o);
+    d += __shfl_xor_sync(0xffffffffu, d, o);
+  }
+  if (lane == 0) {
+    sh[wid] = c;
+    sh[32 + wid] = d;
+  }
   __syncthreads();
-  const double scale0 = sum_partials(B.scale_part, nscale, sh);
-  if (threadIdx.x != 0) return;
-  LMState* lm = B.lm;
+  if (wid != 0) return;
+  c = (lane < nw) ? sh[lane] : 0.0;
+  d = (lane < nw) ? sh[32 + lane] : 0.0;
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    c += __shfl_xor_sync(0xffffffffu, c, o);
+    d += __shfl_xor_sync(0xffffffffu, d, o);
+  }
+  if (lane != 0) return;
+  const double tempChi0 = c, scale0 = d;
+  LMState* lm = &st;
   const double chi_before = lm->current_chi;
   double tempChi = tempChi0;
   if (!lm->solve_ok) tempChi = DBL_MAX;
@@ -895,6 +947,7 @@ __global__ void k_lm_decide(Bufs B, int ncost, int nscale, cudaGraphConditionalH
   // the next trial starts from a successful solve until the factorisation
   // says otherwise
   lm->solve_ok = 1;
+  *B.lm = st;
   if (in_graph) cudaGraphSetConditional(h_trial, more ? 1u : 0u);
 }
 
@@ -1785,7 +1838,7 @@ int solver_upload(Solver* s, const HostProblem& hp, const Structure* hst, Struct
   L.tiles = L.ld / kNB;
   L.nrows = L.ld + 1;  // the b_schur row
   L.ncost = (z.E + 255) / 256;
-  L.nscale_pts = std::max(1, (Lf + 127) / 128);
+  L.nscale_pts = std::max(1, (Lf + kPtsPerBlock - 1) / kPtsPerBlock);
   L.nscale_pose = std::max(1, (Kf + 127) / 128);
   if (L.ld > 4096) {
     if (err) *err = "reduced camera system above 4096 (682 free keyframes)";
