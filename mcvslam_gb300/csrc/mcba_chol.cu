@@ -42,9 +42,14 @@
 //     the working tiles (A, then W = L D after its panel solve), upper
 //     positions (j, i) for L_ij.  Each tile has a version flag: the number of
 //     trailing updates applied (0..j), and j+1 once its panel is solved (for
-//     a diagonal tile, once it is factored).  A producer stores, fences and
-//     releases the flag; a consumer acquires it (bounded wait) and reads the
-//     tile from L2.  Version 0 of every tile is S itself.
+//     a diagonal tile, once it is factored).  A producer stores the tile,
+//     fences and releases the flag; a consumer acquires it (bounded wait)
+//     and reads the tile from L2.  Version 0 of every tile is S itself.  The
+//     flags live in the chain CTA's shared memory and every CTA reaches them
+//     through the cluster's distributed shared memory (release/acquire at
+//     cluster scope): in global memory their polls took the L2 round trip of
+//     whichever die the flag's line maps to, and the factorisation time
+//     depended on that (98 or 104 us at n = 168 on GB300, by the page).
 //   * Backward solve L^T x = y on the chain CTA, block row by block row:
 //     rows of L and M arrive in shared memory by bulk asynchronous copies
 //     (one per tile), and per block row only two 16x16 products lie on the
@@ -59,8 +64,10 @@
 // mbarrier arms) run to completion even then: their producers run whatever
 // the other flags say, so no copy into shared memory is in flight when a CTA
 // leaves.  A pivot <= 0 clears *solve_ok; the
-// chain CTA, which factors every diagonal tile, then leaves x untouched.  No
-// CTA reads another CTA's shared memory.
+// chain CTA, which factors every diagonal tile, then leaves x untouched.
+// Apart from the flags (and the abort word beside them), no CTA reads
+// another CTA's shared memory; a cluster barrier at the end keeps the chain
+// CTA, which holds them, until every CTA is done with them.
 
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
@@ -119,14 +126,16 @@ __device__ __forceinline__ void bar_arrive(int id, int nthreads) {
   asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
+// Flag access at cluster scope (generic addresses into the chain CTA's
+// shared memory, from any CTA of the cluster).
 __device__ __forceinline__ int ld_acquire(const int* p) {
   int v;
-  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  asm volatile("ld.acquire.cluster.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
 
 __device__ __forceinline__ void st_release(int* p, int v) {
-  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+  asm volatile("st.release.cluster.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -217,7 +226,7 @@ __device__ bool wait_ge(const int* p, int v, int* abort_word, bool guard = false
     }
     if (it > 32) __nanosleep(64);
   }
-  atomicExch(abort_word, 1);
+  st_release(abort_word, 1);
   return false;
 }
 
@@ -235,7 +244,7 @@ __device__ void mbar_wait(uint64_t* bar, unsigned parity, int* abort_word) {
         break;
     }
   }
-  atomicExch(abort_word, 1);
+  st_release(abort_word, 1);
 }
 
 // The same for the phase the lookahead worker's pushes complete; that worker
@@ -252,7 +261,7 @@ __device__ void mbar_wait_cluster(uint64_t* bar, unsigned parity, int* abort_wor
         break;
     }
   }
-  atomicExch(abort_word, 1);
+  st_release(abort_word, 1);
 }
 
 struct Geo {
@@ -260,19 +269,20 @@ struct Geo {
   int hold;               // a flag the workers leave unreleased (-1 in every solve; the test of the
                           // bounded waits sets it so that a wait runs out)
   // workspace (doubles): nblk x nblk tiles of 256, then the right-hand-side
-  // rows W, 1/d and y (16 nblk each), then (as ints) the version flags
-  // ((nblk + 1) x nblk), one flag per inverse M_J and the abort word, then
-  // the inverses M_J (256 each, transposed), each part 256-byte aligned
+  // rows W, 1/d and y (16 nblk each), then the inverses M_J (256 each,
+  // transposed), each part 256-byte aligned
   __host__ __device__ size_t tile_off(int i, int j) const { return ((size_t)i * nblk + j) * kTile; }
   __host__ __device__ size_t rhs_w() const { return (size_t)nblk * nblk * kTile; }
   __host__ __device__ size_t rhs_rd() const { return rhs_w() + (size_t)kB * nblk; }
   __host__ __device__ size_t rhs_y() const { return rhs_rd() + (size_t)kB * nblk; }
-  __host__ __device__ size_t flag_offset() const { return ((rhs_y() + (size_t)kB * nblk + 31) / 32) * 32; }
+  __host__ __device__ size_t m_offset() const { return ((rhs_y() + (size_t)kB * nblk + 31) / 32) * 32; }
+  __host__ __device__ size_t ws_doubles() const { return m_offset() + (size_t)nblk * kTile; }
+  // version flags (ints, in the chain CTA's shared memory): one per tile
+  // ((nblk + 1) x nblk, right-hand-side row last), one per inverse M_J, and
+  // the abort word
   __host__ __device__ int inv_index(int J) const { return (nblk + 1) * nblk + J; }
   __host__ __device__ int abort_index() const { return (nblk + 2) * nblk; }
   __host__ __device__ int flag_count() const { return (nblk + 2) * nblk + 1; }
-  __host__ __device__ size_t m_offset() const { return flag_offset() + (((size_t)flag_count() + 63) / 64) * 32; }
-  __host__ __device__ size_t ws_doubles() const { return m_offset() + (size_t)nblk * kTile; }
   // chain CTA shared memory (doubles): two diagonal tiles with 1/d and the
   // squares of the sub-diagonal (step k factors tile D[k & 1] and receives
   // the next one in D[(k+1) & 1]), two incoming panel tiles (P[k & 1]), W
@@ -296,11 +306,11 @@ struct Geo {
   __host__ __device__ size_t w_stage(int b) const { return (size_t)b * (kTile + 2 * kPadTile); }
   __host__ __device__ size_t w_out(int b) const { return w_stage(2) + (size_t)b * 2 * kTile; }
   __host__ __device__ size_t w_end() const { return w_out(2); }
+  // the flags, after everything the chain CTA uses (doubles)
+  __host__ __device__ size_t f_base() const { return c_end() > b_end() ? c_end() : b_end(); }
   __host__ __device__ size_t total() const {
-    size_t t = c_end();
-    if (b_end() > t) t = b_end();
-    if (w_end() > t) t = w_end();
-    return t;
+    const size_t t = f_base() + ((size_t)flag_count() + 1) / 2;
+    return t > w_end() ? t : w_end();
   }
 };
 
@@ -936,7 +946,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_ldlt_cluster(const double* __re
   extern __shared__ __align__(16) double sm[];
   cg::cluster_group cl = cg::this_cluster();
   const int r = (int)cl.block_rank();
-  int* fl = reinterpret_cast<int*>(ws + g.flag_offset());
+  // the flags in the chain CTA's shared memory, seen through the cluster's
+  // shared-memory window
+  int* const fl_local = reinterpret_cast<int*>(sm + g.f_base());
+  int* fl = cl.map_shared_rank(fl_local, 0);
   // the chain CTA's receive mbarriers are ready before any worker can push
   if (r == 0 && threadIdx.x == kMath) {
     mbar_init(reinterpret_cast<uint64_t*>(sm + g.c_rx(0)), 1);
@@ -944,13 +957,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_ldlt_cluster(const double* __re
     fence_mbar_init();
   }
   // the version flags and the abort word start at zero in every launch
-  for (int e = r * kThreads + (int)threadIdx.x; e < g.flag_count(); e += g.C * kThreads) fl[e] = 0;
-  __threadfence();
+  if (r == 0)
+    for (int e = (int)threadIdx.x; e < g.flag_count(); e += kThreads) fl_local[e] = 0;
   cl.sync();
   if (r == 0)
     chain_cta(g, S, ws, x, solve_ok, fl, sm);
   else
     worker_cta(g, S, ws, fl, sm, r);
+  // the chain CTA's shared memory holds the flags: it stays until every CTA
+  // is past its last flag access (a wait that gave up may leave a worker
+  // behind the chain CTA)
+  cl.sync();
 }
 
 Geo make_geo(int C, int ld, int n, int R) {
