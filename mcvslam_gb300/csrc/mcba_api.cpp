@@ -101,7 +101,7 @@ bool finite_arr(const float* a, int n) {
 }
 
 constexpr int kChunk = 256;   // edges per linearisation CTA (one pose per chunk)
-constexpr int kPairChunk = 256;  // Schur pairs per warp task
+constexpr int kPairChunk = 128;  // Schur pairs per warp task
 
 }  // namespace
 

@@ -37,7 +37,7 @@ namespace mcba {
 namespace {
 
 constexpr int kChunk = 256;       // edges per linearisation chunk (one pose per chunk)
-constexpr int kPairChunk = 256;   // Schur pairs per warp task
+constexpr int kPairChunk = 128;   // Schur pairs per warp task
 constexpr int kScanBlock = 1024;  // elements per scan block (256 threads x 4)
 constexpr int kPartTile = 2048;   // keys per partition tile (256 threads x 8 rounds)
 constexpr int kMaxBuckets = 1024;

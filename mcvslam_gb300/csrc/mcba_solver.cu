@@ -494,7 +494,7 @@ __global__ void __launch_bounds__(kLinThreads) k_schur_edge(Bufs B) {
 }
 
 // Reduced-camera block products over the pair list: one warp per chunk of
-// <= 256 pairs that all belong to one block; lanes accumulate whole 6x6
+// <= 128 pairs that all belong to one block; lanes accumulate whole 6x6
 // products in registers, then a reduce-scatter gives one partial per chunk.
 template <typename R>
 __global__ void __launch_bounds__(256) k_schur_pairs(Bufs B, int npc) {
