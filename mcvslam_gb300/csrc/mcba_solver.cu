@@ -540,31 +540,47 @@ __global__ void __launch_bounds__(256) k_schur_pairs(Bufs B, int npc) {
 
 // S_ab = [a == b](Hpp_a + lambda I) - sum of the block's chunk partials, into
 // the dense FP64 reduced camera matrix (lower triangle is what the
-// factorisation reads).
+// factorisation reads).  Four groups of 64 threads each sum a quarter of the
+// block's chunks (36 entries per group), and the quarters meet in a fixed
+// order, so a diagonal block's long run of chunks is four short dependent
+// load chains.  For a diagonal block, group 1 forms b_schur meanwhile.
+constexpr int kAsmGroups = 4;
+
 template <typename R>
-__global__ void k_schur_assemble(Bufs B, int ld) {
+__global__ void __launch_bounds__(64 * kAsmGroups) k_schur_assemble(Bufs B, int ld) {
+  __shared__ Acc<R> sh[kAsmGroups][36];
   const int blk = blockIdx.x;
-  const int t = threadIdx.x;
-  if (t >= 36) return;
+  const int grp = threadIdx.x >> 6, t = threadIdx.x & 63;
   const int a = B.block_ab[2 * blk], bb = B.block_ab[2 * blk + 1];
   const int c0 = B.block_chunk_begin[blk], c1 = B.block_chunk_begin[blk + 1];
-  const Acc<R>* part = reinterpret_cast<const Acc<R>*>(B.ppart);
-  Acc<R> v;
-  v.zero();
-  acc_range(v, part + t, c0, c1, 36);
+  if (t < 36) {
+    const int len = c1 - c0;
+    const int g0 = c0 + (int)(((long long)len * grp) / kAsmGroups);
+    const int g1 = c0 + (int)(((long long)len * (grp + 1)) / kAsmGroups);
+    const Acc<R>* part = reinterpret_cast<const Acc<R>*>(B.ppart);
+    Acc<R> v;
+    v.zero();
+    acc_range(v, part + t, g0, g1, 36);
+    sh[grp][t] = v;
+  }
+  if (a == bb && grp == 1 && t < 6) {
+    // b_schur = b_p - sum of the pose's q chunk partials
+    const Acc<R>* qp = reinterpret_cast<const Acc<R>*>(B.qpart);
+    Acc<R> qs;
+    qs.zero();
+    acc_range(qs, qp + t, B.pose_chunk_begin[a], B.pose_chunk_begin[a + 1], 6);
+    B.S[(size_t)ld * ld + 6 * a + t] = B.bp[6 * (size_t)a + t] - qs.value();
+  }
+  __syncthreads();
+  if (grp != 0 || t >= 36) return;
+  Acc<R> v = sh[0][t];
+#pragma unroll
+  for (int g = 1; g < kAsmGroups; ++g) v.add(sh[g][t]);
   const int r = t / 6, q = t % 6;
   if (a == bb) {
     double d = B.Hpp[(size_t)a * 36 + t] - v.value();
     if (r == q) d += B.lm->lambda;
     B.S[(size_t)(6 * a + r) * ld + 6 * a + q] = d;
-    if (t < 6) {
-      // b_schur = b_p - sum of the pose's q chunk partials
-      const Acc<R>* qp = reinterpret_cast<const Acc<R>*>(B.qpart);
-      Acc<R> qs;
-      qs.zero();
-      acc_range(qs, qp + t, B.pose_chunk_begin[a], B.pose_chunk_begin[a + 1], 6);
-      B.S[(size_t)ld * ld + 6 * a + t] = B.bp[6 * (size_t)a + t] - qs.value();
-    }
   } else {
     const double d = -v.value();
     B.S[(size_t)(6 * a + r) * ld + 6 * bb + q] = d;
@@ -1434,7 +1450,7 @@ void launch_trial(Solver* s, const Bufs& B, const Launch& L, PhaseClock& pc, cud
       }
     });
     pc.run(MCBA_PHASE_SCHUR_ASSEMBLE, [&] {
-      k_schur_assemble<R><<<L.nblk, 64, 0, st>>>(B, L.ld);
+      k_schur_assemble<R><<<L.nblk, 64 * kAsmGroups, 0, st>>>(B, L.ld);
       s->launches++;
     });
     pc.run(MCBA_PHASE_CHOLESKY, [&] {
