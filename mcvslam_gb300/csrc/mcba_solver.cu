@@ -45,7 +45,15 @@ using namespace dev;
 
 namespace {
 
-constexpr int kRow = 28;   // per canonical edge: Hpl 6x3 | Hll upper 6 | b_l 3 | pad
+// Per canonical edge row: Hpl 6x3 | Hll upper 6 | b_l 3 | pad = 28 reals.  FP32
+// rows append the low halves of the float-float Hll terms (28..33) and pad
+// to 36 floats (144 B, a multiple of 16 B).
+template <typename R>
+__host__ __device__ constexpr int row_stride() {
+  return sizeof(R) == sizeof(double) ? 28 : 36;
+}
+constexpr int kHllLo = 28;
+constexpr int kPdv = 12;   // per free point: (Hll + lambda I)^-1 row-major 9 | Dinv b_l 3
 constexpr int kYQ = 24;    // per canonical edge: Y 6x3 | q 6
 constexpr int kNB = 32;    // Cholesky tile
 constexpr int kLinThreads = 256;
@@ -91,12 +99,13 @@ struct Bufs {
   int* free_pose_ids;
   int* free_point_ids;
   // numeric workspaces (R-typed, stored as bytes)
-  void* rows;       // [Ec][kRow]
+  void* rows;       // [Ec][row_stride<R>()]
   void* partials;   // [nchunk][32] accumulators
   double* Hpp;      // [Kf][36] FP64 (formed from the accumulators)
-  void* Hll;        // [Lf][6]
+  double* Hll;      // [Lf][6] FP64 (upper triangle of the point blocks)
   double* bp;       // [6Kf] FP64
   void* bl;         // [3Lf]
+  void* pdv;        // [Lf][kPdv] damped point-block inverses of the current trial
   void* yq;         // [Ec][kYQ]
   void* ppart;      // [npchunk][36] accumulators
   void* qpart;      // [nchunk][6] accumulators of Hpl Dinv b_l per pose chunk
@@ -166,10 +175,80 @@ __device__ __forceinline__ void store_row<double, 20>(double* p, const double* v
   for (int i = 0; i < 10; ++i) q[i] = make_double2(v[2 * i], v[2 * i + 1]);
 }
 template <>
-__device__ __forceinline__ void store_row<float, 28>(float* p, const float* v) {
+__device__ __forceinline__ void store_row<float, 36>(float* p, const float* v) {
   float4* q = reinterpret_cast<float4*>(p);
 #pragma unroll
-  for (int i = 0; i < 7; ++i) q[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+  for (int i = 0; i < 9; ++i) q[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+}
+template <>
+__device__ __forceinline__ void store_row<float, 12>(float* p, const float* v) {
+  float4* q = reinterpret_cast<float4*>(p);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) q[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+}
+template <>
+__device__ __forceinline__ void store_row<double, 12>(double* p, const double* v) {
+  double2* q = reinterpret_cast<double2*>(p);
+#pragma unroll
+  for (int i = 0; i < 6; ++i) q[i] = make_double2(v[2 * i], v[2 * i + 1]);
+}
+template <>
+__device__ __forceinline__ void load_row<float, 12>(const float* p, float* v) {
+  const float4* q = reinterpret_cast<const float4*>(p);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float4 t = q[i];
+    v[4 * i] = t.x;
+    v[4 * i + 1] = t.y;
+    v[4 * i + 2] = t.z;
+    v[4 * i + 3] = t.w;
+  }
+}
+template <>
+__device__ __forceinline__ void load_row<double, 12>(const double* p, double* v) {
+  const double2* q = reinterpret_cast<const double2*>(p);
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    const double2 t = q[i];
+    v[2 * i] = t.x;
+    v[2 * i + 1] = t.y;
+  }
+}
+
+// w * sum_k Jl[k][i] Jl[k][q] over the residual rows: one entry of an edge's
+// point block.  FP64 rows evaluate it directly.  FP32 rows carry it as an
+// unevaluated float-float pair (hi + lo): every product is split exactly by an
+// FMA (TwoProduct) and the terms are added with TwoSum, all on FP32 pipes.
+// The block of a point seen along nearly parallel rays is ill-conditioned, and
+// its inverse enlarges the rounding of single FP32 entries by the condition
+// number; the pair keeps those bits until the FP64 per-point sum.
+template <typename R>
+__device__ __forceinline__ void hll_entry(const R (&Jl)[3][3], R w, bool d3, int i, int q, R& hi, R& lo);
+template <>
+__device__ __forceinline__ void hll_entry<double>(const double (&Jl)[3][3], double w, bool d3, int i, int q,
+                                                  double& hi, double& lo) {
+  double h = (Jl[0][i] * w) * Jl[0][q] + (Jl[1][i] * w) * Jl[1][q];
+  if (d3) h += (Jl[2][i] * w) * Jl[2][q];
+  hi = h;
+  lo = 0.0;
+}
+template <>
+__device__ __forceinline__ void hll_entry<float>(const float (&Jl)[3][3], float w, bool d3, int i, int q, float& hi,
+                                                 float& lo) {
+  Acc<float> a;
+  a.zero();
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    if (k == 2 && !d3) break;
+    const float ah = __fmul_rn(Jl[k][i], w);
+    const float al = __fmaf_rn(Jl[k][i], w, -ah);       // Jl_i w = ah + al exactly
+    const float ph = __fmul_rn(ah, Jl[k][q]);
+    const float pl = __fadd_rn(__fmaf_rn(ah, Jl[k][q], -ph), __fmul_rn(al, Jl[k][q]));
+    a.add(ph);
+    a.lo = __fadd_rn(a.lo, pl);
+  }
+  hi = __fadd_rn(a.hi, a.lo);
+  lo = __fsub_rn(a.lo, __fsub_rn(hi, a.hi));
 }
 template <>
 __device__ __forceinline__ void store_row<double, 28>(double* p, const double* v) {
@@ -240,8 +319,8 @@ __global__ void __launch_bounds__(kLinThreads) k_linearize(Bufs B) {
 #pragma unroll
       for (int i = 0; i < 6; ++i) wJp[k][i] = (k < 2 || d3) ? Jp[k][i] * w : R(0);
     if (r.point_h >= 0) {
-      R* row = Ptrs<R>::p(B.rows) + (size_t)r.canon * kRow;
-      R out[kRow];
+      R* row = Ptrs<R>::p(B.rows) + (size_t)r.canon * row_stride<R>();
+      R out[row_stride<R>()];
 #pragma unroll
       for (int i = 0; i < 6; ++i)
 #pragma unroll
@@ -257,16 +336,18 @@ __global__ void __launch_bounds__(kLinThreads) k_linearize(Bufs B) {
       for (int i = 0; i < 3; ++i) {
 #pragma unroll
         for (int q = i; q < 3; ++q) {
-          R h = (Jl[0][i] * w) * Jl[0][q] + (Jl[1][i] * w) * Jl[1][q];
-          if (d3) h += (Jl[2][i] * w) * Jl[2][q];
-          out[18 + u3(i, q)] = h;
+          R lo;
+          hll_entry<R>(Jl, w, d3, i, q, out[18 + u3(i, q)], lo);
+          if constexpr (row_stride<R>() > kHllLo) out[kHllLo + u3(i, q)] = lo;
         }
         R bb = Jl[0][i] * om[0] + Jl[1][i] * om[1];
         if (d3) bb += Jl[2][i] * om[2];
         out[24 + i] = bb;
       }
       out[27] = R(0);
-      store_row<R, kRow>(row, out);
+#pragma unroll
+      for (int k = kHllLo + 6; k < row_stride<R>(); ++k) out[k] = R(0);
+      store_row<R, row_stride<R>()>(row, out);
     }
     if (r.pose_h >= 0) {
 #pragma unroll
@@ -340,25 +421,35 @@ __device__ __forceinline__ void pose_reduce_warp(const Bufs& B, int Kf, int i, i
 }
 
 // Hll / b_l: sum over the (<= a few) edges of each free point.
+// Hll is summed in FP64 (from the float-float pairs of FP32 rows), b_l in
+// the linearisation type.
 template <typename R>
 __device__ __forceinline__ void point_reduce_thread(const Bufs& B, int Lf, int l) {
   if (l >= Lf) return;
   const int e0 = B.pt_begin[l], e1 = B.pt_begin[l + 1];
-  R s[9];
+  double h[6];
+  R s[3];
 #pragma unroll
-  for (int k = 0; k < 9; ++k) s[k] = R(0);
+  for (int k = 0; k < 6; ++k) h[k] = 0.0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) s[k] = R(0);
 #pragma unroll 4
   for (int e = e0; e < e1; ++e) {
-    const R* row = Ptrs<R>::p(B.rows) + (size_t)e * kRow + 18;
+    const R* row = Ptrs<R>::p(B.rows) + (size_t)e * row_stride<R>();
 #pragma unroll
-    for (int k = 0; k < 9; ++k) s[k] += row[k];
+    for (int k = 0; k < 6; ++k) {
+      h[k] += (double)row[18 + k];
+      if constexpr (row_stride<R>() > kHllLo) h[k] += (double)row[kHllLo + k];
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) s[k] += row[24 + k];
   }
-  R* H = Ptrs<R>::p(B.Hll) + (size_t)l * 6;
+  double* H = B.Hll + (size_t)l * 6;
 #pragma unroll
-  for (int k = 0; k < 6; ++k) H[k] = s[k];
+  for (int k = 0; k < 6; ++k) H[k] = h[k];
   R* b = Ptrs<R>::p(B.bl) + 3 * (size_t)l;
 #pragma unroll
-  for (int k = 0; k < 3; ++k) b[k] = s[6 + k];
+  for (int k = 0; k < 3; ++k) b[k] = s[k];
 }
 
 // Both reductions in one launch of 128-thread blocks: the first blocks take
@@ -393,7 +484,7 @@ __global__ void k_lambda_max(Bufs B, int Kf, int Lf) {
       v = abs_bits(B.Hpp[(size_t)(k / 6) * 36 + 7 * (k % 6)]);
     } else {
       const int i = k - 6 * Kf, d = i % 3;
-      v = abs_bits((double)Ptrs<R>::p(B.Hll)[(size_t)(i / 3) * 6 + (d == 0 ? 0 : d == 1 ? 3 : 5)]);
+      v = abs_bits(B.Hll[(size_t)(i / 3) * 6 + (d == 0 ? 0 : d == 1 ? 3 : 5)]);
     }
     m = v > m ? v : m;
   }
@@ -436,6 +527,26 @@ __device__ __forceinline__ void damped_inverse(const R* Hu, R lam, R* Di) {
   Di[8] = (d00 * d11 - d01 * d01) * id;
 }
 
+// (Hll + lambda I)^-1 and Dinv b_l of every free point for the current trial
+// (block_solver.hpp:346-354 inverts each landmark's damped block), in FP64
+// from the FP64 point blocks, stored in the linearisation type:
+// pdv[l] = Dinv row-major (9) | Dinv b_l (3).
+template <typename R>
+__global__ void __launch_bounds__(128) k_point_dinv(Bufs B, int Lf) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= Lf) return;
+  double D[9];
+  damped_inverse<double>(B.Hll + (size_t)l * 6, B.lm->lambda, D);
+  const R* bl = Ptrs<R>::p(B.bl) + 3 * (size_t)l;
+  const double b0 = (double)bl[0], b1 = (double)bl[1], b2 = (double)bl[2];
+  R o[kPdv];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) o[k] = (R)D[k];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) o[9 + i] = (R)(D[3 * i] * b0 + D[3 * i + 1] * b1 + D[3 * i + 2] * b2);
+  store_row<R, kPdv>(Ptrs<R>::p(B.pdv) + (size_t)l * kPdv, o);
+}
+
 // Y_e = Hpl_e Dinv for every edge with a free point and a free pose, walked in
 // the pose-sorted stream (one pose per CTA) so that q = sum_e Hpl_e Dinv b_l
 // -- the coefficient subtracted from b_p (block_solver.hpp:356-374) -- is
@@ -453,15 +564,11 @@ __global__ void __launch_bounds__(kLinThreads) k_schur_edge(Bufs B) {
     const EdgeRec r = B.recs[j];
     if (r.canon >= 0 && r.pose_h >= 0) {
       const int e = r.canon, l = r.point_h;
-      const R lam = (R)B.lm->lambda;
-      R Di[9];
-      damped_inverse<R>(Ptrs<R>::p(B.Hll) + (size_t)l * 6, lam, Di);
-      const R* bl = Ptrs<R>::p(B.bl) + 3 * (size_t)l;
-      R db[3];
-#pragma unroll
-      for (int i = 0; i < 3; ++i) db[i] = Di[3 * i] * bl[0] + Di[3 * i + 1] * bl[1] + Di[3 * i + 2] * bl[2];
+      R Di[kPdv];
+      load_row<R, kPdv>(Ptrs<R>::p(B.pdv) + (size_t)l * kPdv, Di);
+      const R* db = Di + 9;
       R h[20];
-      load_row<R, 20>(Ptrs<R>::p(B.rows) + (size_t)e * kRow, h);
+      load_row<R, 20>(Ptrs<R>::p(B.rows) + (size_t)e * row_stride<R>(), h);
       R y[20];
 #pragma unroll
       for (int rr = 0; rr < 6; ++rr) {
@@ -512,7 +619,7 @@ __global__ void __launch_bounds__(256) k_schur_pairs(Bufs B, int npc) {
   for (int p = p0 + lane; p < p1; p += 32) {
     const int2 ij = B.pairs[p];
     const R* Y = yq + (size_t)ij.x * kYQ;
-    const R* H = rows + (size_t)ij.y * kRow;
+    const R* H = rows + (size_t)ij.y * row_stride<R>();
     R y[20], h[20];
     load_row<R, 20>(Y, y);
     load_row<R, 20>(H, h);
@@ -736,7 +843,7 @@ __device__ __forceinline__ void backsub_block(const Bufs& B, int Lf, int n, int 
     for (int e = B.pt_begin[l] + sub; e < e1; e += kPtLanes) {
       const int ph = B.canon_pose_h[e];
       if (ph < 0) continue;
-      const R* H = Ptrs<R>::p(B.rows) + (size_t)e * kRow;
+      const R* H = Ptrs<R>::p(B.rows) + (size_t)e * row_stride<R>();
       const double* xp = B.x + 6 * (size_t)ph;
       R xr[6];
 #pragma unroll
@@ -762,9 +869,8 @@ __device__ __forceinline__ void backsub_block(const Bufs& B, int Lf, int n, int 
     double* xl = B.x + n + 3 * (size_t)l;
     if (ok) {
       const R cl[3] = {bl[0] - t[0], bl[1] - t[1], bl[2] - t[2]};
-      R Di[9];
-      damped_inverse<R>(Ptrs<R>::p(B.Hll) + (size_t)l * 6, (R)lam, Di);
-      xl[q] = (double)(Di[3 * q] * cl[0] + Di[3 * q + 1] * cl[1] + Di[3 * q + 2] * cl[2]);
+      const R* Dq = Ptrs<R>::p(B.pdv) + (size_t)l * kPdv + 3 * q;  // row q of Dinv
+      xl[q] = (double)(Dq[0] * cl[0] + Dq[1] * cl[1] + Dq[2] * cl[2]);
     }
     const int id = B.free_point_ids[l];
     const double d = xl[q];
@@ -1055,7 +1161,7 @@ class Solver {
       block_ab, block_chunk_begin, pose_canon_begin, pose_canon_list, free_pose_ids, free_point_ids;
   DBuf<int2> pairs;
   // numerics
-  DBuf<char> rows, partials, Hll, bl, yq, ppart, qpart;
+  DBuf<char> rows, partials, Hll, bl, pdv, yq, ppart, qpart;
   DBuf<double> Hpp, bp, S, cws, dinv, x, cost_part, scale_part, chi2_out;
   DBuf<LMState> lm;
   DBuf<mcba_trial_log> log;
@@ -1121,7 +1227,7 @@ class Solver {
                        &free_pose_ids, &free_point_ids};
     for (auto* d : is) d->release();
     pairs.release();
-    DBuf<char>* cs[] = {&rows, &partials, &Hll, &bl, &yq, &ppart, &qpart};
+    DBuf<char>* cs[] = {&rows, &partials, &Hll, &bl, &pdv, &yq, &ppart, &qpart};
     for (auto* d : cs) d->release();
     lm.release();
     log.release();
@@ -1362,7 +1468,8 @@ Bufs make_bufs(Solver* s) {
   B.Hpp = s->Hpp.p;
   B.bp = s->bp.p;
   B.bl = s->bl.p;
-  B.Hll = s->Hll.p;
+  B.Hll = reinterpret_cast<double*>(s->Hll.p);
+  B.pdv = s->pdv.p;
   B.yq = s->yq.p;
   B.ppart = s->ppart.p;
   B.qpart = s->qpart.p;
@@ -1438,6 +1545,12 @@ template <typename R>
 void launch_trial(Solver* s, const Bufs& B, const Launch& L, PhaseClock& pc, cudaGraphConditionalHandle h_trial,
                   int in_graph) {
   cudaStream_t st = s->stream;
+  if (L.Lf) {
+    pc.run(MCBA_PHASE_SCHUR_EDGE, [&] {
+      k_point_dinv<R><<<(L.Lf + 127) / 128, 128, 0, st>>>(B, L.Lf);
+      s->launches++;
+    });
+  }
   if (L.Kf) {
     pc.run(MCBA_PHASE_SCHUR_EDGE, [&] {
       k_schur_edge<R><<<L.nchunk, kLinThreads, 0, st>>>(B);
@@ -1500,12 +1613,13 @@ int alloc_numerics(Solver* s, std::string* err) {
   const Launch& L = s->L;
   const size_t rb = sizeof(R);
   const int nx = L.n + 3 * L.Lf;
-  CK(s->rows.ensure(std::max<size_t>(1, (size_t)L.Ec * kRow * rb)));
+  CK(s->rows.ensure(std::max<size_t>(1, (size_t)L.Ec * row_stride<R>() * rb)));
   const size_t ab = sizeof(Acc<R>);
   CK(s->partials.ensure(std::max<size_t>(1, (size_t)L.nchunk * 32 * ab)));
   CK(s->Hpp.ensure(std::max<size_t>(1, (size_t)L.Kf * 36)));
   CK(s->bp.ensure(std::max<size_t>(1, (size_t)L.Kf * 6)));
-  CK(s->Hll.ensure(std::max<size_t>(1, (size_t)L.Lf * 6 * rb)));
+  CK(s->Hll.ensure(std::max<size_t>(1, (size_t)L.Lf * 6 * sizeof(double))));
+  CK(s->pdv.ensure(std::max<size_t>(1, (size_t)L.Lf * kPdv * rb)));
   CK(s->bl.ensure(std::max<size_t>(1, (size_t)L.Lf * 3 * rb)));
   CK(s->yq.ensure(std::max<size_t>(1, (size_t)L.Ec * kYQ * rb)));
   CK(s->ppart.ensure(std::max<size_t>(1, (size_t)L.npc * 36 * ab)));

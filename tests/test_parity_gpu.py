@@ -87,6 +87,53 @@ def test_pose_only_rounds_match_oracle(gpu):
     assert rot_diff(qt[0, :4], o["pose_qt"][0, :4]) <= POSE_TOL_RAD
 
 
+def _unary_problem(name):
+    """EdgeSE3XYZ2CameraOnlyPose (include/OptimizeTypes.hpp:20-68) problems:
+    every edge unary (the point is a constant of the edge), or every ninth
+    edge of config 1 unary beside binary edges."""
+    if name == "unary":
+        pr = synth.pose_only(800, seed=5)
+        pr.edge_type[:] = synth.EDGE_UNARY
+        return pr
+    pr = synth.config(1)
+    pr.edge_type[::9] = synth.EDGE_UNARY
+    return pr
+
+
+@pytest.mark.parametrize("name,iters", [("unary", 4), ("mixed_types", 10)])
+def test_unary_edges_follow_oracle_trial_by_trial(name, iters, gpu):
+    """Unary edges build their 6x6 pose block and b_p term only
+    (base_unary_edge.hpp:51-79); FP64 plain follows the oracle trial by trial.
+    The single-pose problem has converged to the last bits after about five
+    iterations; beyond that the gain ratio of a trial is rounding noise
+    (|rho| ~ 1e-8 on a cost change of 1e-10) and the accept/reject decision is
+    not a property of the algorithm, so it is compared over four."""
+    pr = _unary_problem(name)
+    o = oracle.optimize(pr, iters)
+    g = ba.solve(pr, iters, "fp64")
+    assert g["stats"]["iterations"] == o["ret"]
+    compare_logs(g["log"], o["log"])
+    assert abs(g["stats"]["final_chi2"] - o["final_chi2"]) <= CHI_RTOL * o["final_chi2"]
+    compare_state(g, o, pr)
+
+
+def test_unary_pose_only_rounds_match_oracle(gpu):
+    """PoseOptimization's four rounds (src/PoseEstimation.cpp:48-130) over unary
+    edges: inlier count, written flag, per-edge levels and the final pose."""
+    pr = synth.pose_only(1200, seed=43)
+    pr.edge_type[:] = synth.EDGE_UNARY
+    o = oracle.pose_optimization(pr, rounds=4, iters=10, chi2_thr=5.991)
+    with ba.Solver() as s:
+        s.load(pr)
+        inl, written = s.pose_optimization(4, 10, 5.991, 2)
+        lv = s.levels()
+        qt, _ = s.state()
+    assert inl == o["ret"] and written == o["pose_written"]
+    np.testing.assert_array_equal(lv, o["edge_level"])
+    assert np.abs(qt[0, 4:] - o["pose_qt"][0, 4:]).max() <= POSE_TOL_M
+    assert rot_diff(qt[0, :4], o["pose_qt"][0, :4]) <= POSE_TOL_RAD
+
+
 def test_local_ba_filter_matches_oracle(gpu):
     pr = synth.config(1)
     o = oracle.local_ba(pr, 10)
@@ -98,13 +145,13 @@ def test_local_ba_filter_matches_oracle(gpu):
     np.testing.assert_array_equal(lv, o["edge_level"])
 
 
-@pytest.mark.parametrize("cfg,iters", [(1, 10), (2, 20)])
+@pytest.mark.parametrize("cfg,iters", [(1, 10), (2, 10), (2, 20), (5, 20)])
 def test_mixed_precision_final_cost_gap(cfg, iters, gpu):
-    """Final cost of the mixed-precision solve, evaluated in FP64, within 1e-6 of
-    the FP64 solve.  Config 2 is compared after 20 iterations: at 10 its LM path
-    still trails by ~6e-6 (FP32 Jacobians perturb the steps along the weakly
-    conditioned directions once lambda is small); both paths reach the same
-    cost by iteration 20."""
+    """Final cost of the mixed-precision solve, evaluated in FP64, within 1e-6
+    (either side) of the FP64 solve after the same iterations.  The FP32 point
+    blocks are carried as float-float pairs and inverted in FP64: rounded to
+    single FP32 entries they moved the config-2 path by 6e-6 at 10 iterations
+    (the inverse of an ill-conditioned 3x3 block enlarges their rounding)."""
     pr = synth.config(cfg)
     plain = ba.solve(pr, iters, "fp64")
     mixed = ba.solve(pr, iters, "mixed")
@@ -116,7 +163,7 @@ def test_mixed_precision_final_cost_gap(cfg, iters, gpu):
     chi_mixed = st["initial_chi2"]
     chi_plain = plain["stats"]["final_chi2"]
     gap = (chi_mixed - chi_plain) / chi_plain
-    assert gap <= 1e-6, gap
+    assert abs(gap) <= 1e-6, gap
     terr = np.abs(mixed["pose_qt"][:, 4:] - plain["pose_qt"][:, 4:]).max()
     assert terr < 1e-3
 
@@ -291,6 +338,22 @@ def test_cluster_solve_up_to_its_largest_size_follows_oracle(n_kf, gpu):
     g = ba.solve(pr, 5, "fp64")
     assert g["stats"]["iterations"] == o["ret"]
     compare_logs(g["log"], o["log"])
+    compare_state(g, o, pr)
+
+
+def test_config5_fp64_follows_oracle_trial_by_trial(gpu):
+    """The large map (300 keyframes, 200k points, 1.6M edges): a reduced
+    camera system of 1788 unknowns through the tiled factorisation, three LM
+    iterations trial by trial against the multi-threaded oracle."""
+    import os
+
+    pr = synth.config(5)
+    o = oracle.optimize(pr, 3, n_threads=os.cpu_count() or 1)
+    g = ba.solve(pr, 3, "fp64")
+    assert g["stats"]["n_free_poses"] * 6 == 1788
+    assert g["stats"]["iterations"] == o["ret"]
+    compare_logs(g["log"], o["log"])
+    assert abs(g["stats"]["final_chi2"] - o["final_chi2"]) <= CHI_RTOL * o["final_chi2"]
     compare_state(g, o, pr)
 
 
