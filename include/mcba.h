@@ -458,7 +458,11 @@ int mcba_reproj_backward(int32_t double_precision, int64_t n, const void* pose_q
  * calls on a device: n is limited to MCBA_NOALLOC_MAX_EDGES (larger n returns
  * MCBA_ERR_TOO_LARGE) and calls that overlap on the GPU race on the array.
  * The first call on a device looks the array's device address up; make that
- * call before any stream capture on the device.
+ * call before any stream capture on the device.  The address it keeps is that
+ * of the device's context at the time: after cudaDeviceReset of a device, make
+ * no further call on that device in the same process.  A CUDA error already
+ * pending on the calling thread is left in place and the call returns
+ * MCBA_ERR_CUDA without launching.
  * Inputs (device pointers): pose_qt [n][7] T_body_world, ext_qt [n][7]
  * T_cam_body, X [n][3], K [n][4], obs [n][2], info [n] (NULL: 1), delta [n]
  * Huber threshold (NULL or <= 0: no kernel), robust [n] (NULL: all robust).

@@ -23,6 +23,7 @@
 
 #include <cstdint>
 #include <functional>
+#include <limits>
 #include <string>
 #include <unordered_map>
 #include <utility>
@@ -44,7 +45,14 @@ class BAoptimizer {
     int level() const { return opt->levels_[id]; }
     void setLevel(int lv) { opt->levels_[id] = (uint8_t)lv; opt->dirty_levels_ = true; }
     void computeError() { opt->refresh_chi2(); }
-    double chi2() const { return opt->chi2_[id]; }
+    // g2o's chi2() returns the value of the last computeError(); here the
+    // per-edge values are evaluated on first use after optimize()/filter()
+    // at the current estimates, so chi2() is valid without a prior
+    // computeError().  NaN if the evaluation failed (see status()).
+    double chi2() {
+      opt->refresh_chi2();
+      return opt->chi2_ok_ ? opt->chi2_[id] : std::numeric_limits<double>::quiet_NaN();
+    }
     void setRobustKernel(bool on) { opt->robust_[id] = on ? 1 : 0; opt->dirty_robust_ = true; }
   };
   struct EdgeInfo {
@@ -176,7 +184,11 @@ class BAoptimizer {
     if (chi2_.size() == levels_.size()) return;
     sync_flags();
     chi2_.assign(levels_.size(), 0.0);
-    if (!chi2_.empty()) status_ = mcba_edge_chi2(p_, chi2_.data());
+    chi2_ok_ = true;
+    if (!chi2_.empty()) {
+      status_ = mcba_edge_chi2(p_, chi2_.data());
+      chi2_ok_ = status_ == MCBA_OK;
+    }
   }
   void sync_flags() {
     if (dirty_levels_ && !levels_.empty()) mcba_set_edge_levels(p_, levels_.data());
@@ -190,6 +202,7 @@ class BAoptimizer {
   MPAccess mpa_;
   std::vector<uint8_t> levels_, robust_;
   std::vector<double> chi2_;
+  bool chi2_ok_ = false;
   std::vector<EdgeInfo> infos_;
   bool dirty_levels_ = false, dirty_robust_ = false;
 };

@@ -21,6 +21,14 @@
 // stand-in symbol, not a device address.  The first call on each device looks
 // up the real address with cudaGetSymbolAddress (with that device current) and
 // caches it; make that first call before any stream capture on the device.
+// The cached address belongs to the device's context at that time: after a
+// cudaDeviceReset of a device, no further call may be made on that device in
+// the same process (the array is reloaded at a new address the cache does not
+// know).
+//
+// Error reporting: a CUDA error already pending on the calling thread when the
+// call starts is left in place and the call returns MCBA_ERR_CUDA without
+// launching; otherwise each launch is checked on its own.
 
 #include <cuda_runtime.h>
 
@@ -137,14 +145,19 @@ extern "C" int mcba_robust_cost_noalloc(int64_t n, const double* pose_qt, const 
   if (n < 0 || !cost) return MCBA_ERR_INVALID;
   if (n > MCBA_NOALLOC_MAX_EDGES) return MCBA_ERR_TOO_LARGE;
   if (n > 0 && (!pose_qt || !ext_qt || !X || !K || !obs)) return MCBA_ERR_INVALID;
+  // an error left by an earlier, unrelated call stays with the caller
+  if (cudaPeekAtLastError() != cudaSuccess) return MCBA_ERR_CUDA;
   double* partials = nullptr;
   const int r = partials_address(&partials);
   if (r != MCBA_OK) return r;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int nblocks = (int)((n + kNoAllocThreads - 1) / kNoAllocThreads);
-  if (nblocks > 0)
+  if (nblocks > 0) {
     k_cost_partials_noalloc<<<nblocks, kNoAllocThreads, 0, st>>>(n, pose_qt, ext_qt, X, K, obs, info, delta, robust,
                                                                  partials);
+    if (cudaGetLastError() != cudaSuccess) return MCBA_ERR_CUDA;
+  }
   k_cost_total_noalloc<<<1, 256, 0, st>>>(partials, nblocks, cost);
-  return cudaGetLastError() == cudaSuccess ? MCBA_OK : MCBA_ERR_CUDA;
+  if (cudaGetLastError() != cudaSuccess) return MCBA_ERR_CUDA;
+  return MCBA_OK;
 }

@@ -16,39 +16,44 @@ extern "C" int chol_probe_solve(const double* S_host, int n, int ld, double* x_h
   const size_t total = (size_t)(ld + 32) * ld;
   double *S = nullptr, *ws = nullptr, *x = nullptr;
   int* ok = nullptr;
-  cudaEvent_t e0, e1;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
   int rc = 0;
-  if (cudaMalloc(&S, total * sizeof(double)) || cudaMalloc(&ws, total * sizeof(double)) ||
-      cudaMalloc(&x, (size_t)ld * sizeof(double)) || cudaMalloc(&ok, sizeof(int)))
-    return -2;
   const int one = 1;
-  cudaMemcpy(S, S_host, total * sizeof(double), cudaMemcpyHostToDevice);
-  cudaMemcpy(x, x_host, (size_t)ld * sizeof(double), cudaMemcpyHostToDevice);
-  cudaMemcpy(ok, &one, sizeof(int), cudaMemcpyHostToDevice);
-  Geo g = make_geo(plan.cluster, ld, n, plan.slots);
-  if (hold) g.hold = g.nblk * g.nblk;  // flag of right-hand-side panel (nblk, 0)
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(plan.cluster, 1, 1);
-  cfg.blockDim = dim3(kThreads, 1, 1);
-  cfg.dynamicSmemBytes = plan.smem_bytes;
-  cudaLaunchAttribute attr;
-  attr.id = cudaLaunchAttributeClusterDimension;
-  attr.val.clusterDim.x = plan.cluster;
-  attr.val.clusterDim.y = 1;
-  attr.val.clusterDim.z = 1;
-  cfg.attrs = &attr;
-  cfg.numAttrs = 1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  cudaEventRecord(e0);
-  if (cudaLaunchKernelEx(&cfg, k_ldlt_cluster, (const double*)S, ws, x, ok, g) != cudaSuccess) rc = -3;
-  cudaEventRecord(e1);
-  if (cudaDeviceSynchronize() != cudaSuccess) rc = -4;
-  cudaEventElapsedTime(ms, e0, e1);
-  cudaMemcpy(x_host, x, (size_t)ld * sizeof(double), cudaMemcpyDeviceToHost);
-  cudaMemcpy(solve_ok, ok, sizeof(int), cudaMemcpyDeviceToHost);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
+  // every early exit below goes through the frees at the end
+  if (cudaMalloc(&S, total * sizeof(double)) != cudaSuccess || cudaMalloc(&ws, total * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&x, (size_t)ld * sizeof(double)) != cudaSuccess || cudaMalloc(&ok, sizeof(int)) != cudaSuccess) {
+    rc = -2;
+  } else if (cudaMemcpy(S, S_host, total * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+             cudaMemcpy(x, x_host, (size_t)ld * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+             cudaMemcpy(ok, &one, sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
+    rc = -5;
+  } else if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    rc = -6;
+  } else {
+    Geo g = make_geo(plan.cluster, ld, n, plan.slots);
+    if (hold) g.hold = g.nblk * g.nblk;  // flag of right-hand-side panel (nblk, 0)
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(plan.cluster, 1, 1);
+    cfg.blockDim = dim3(kThreads, 1, 1);
+    cfg.dynamicSmemBytes = plan.smem_bytes;
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = plan.cluster;
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    cudaEventRecord(e0);
+    if (cudaLaunchKernelEx(&cfg, k_ldlt_cluster, (const double*)S, ws, x, ok, g) != cudaSuccess) rc = -3;
+    cudaEventRecord(e1);
+    if (cudaDeviceSynchronize() != cudaSuccess) rc = -4;
+    if (rc == 0 && cudaEventElapsedTime(ms, e0, e1) != cudaSuccess) rc = -7;
+    if (rc == 0 && (cudaMemcpy(x_host, x, (size_t)ld * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
+                    cudaMemcpy(solve_ok, ok, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess))
+      rc = -5;
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
   cudaFree(S);
   cudaFree(ws);
   cudaFree(x);
