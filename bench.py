@@ -1,16 +1,21 @@
 """Benchmark: LM edges linearised per second of a multi-camera local BA.
 
-Workload (one "step"): a full 10-iteration Levenberg-Marquardt local bundle
-adjustment of the 30-keyframe x 3-camera window with 20k map points
-(~150k observations, 5% outliers, Huber sqrt(5.991), first 2 keyframes fixed),
-solved on one GPU by libmcba.  Metric: active edges x LM iterations / solve
-time.  Seeded synthetic data with the benchmark's shapes and noise model.
+Workload (one "step"): a full Levenberg-Marquardt local bundle adjustment
+(10 iterations; 20 for the large map) of the 30-keyframe x 3-camera window with
+20k map points (~150k observations, 5% outliers, Huber sqrt(5.991), first 2
+keyframes fixed), solved on one GPU by libmcba in mixed precision.  Metric:
+active edges x LM iterations / solve time.  Seeded synthetic data with the
+benchmark's shapes and noise model.
 
   value   device-resident: problem compiled and uploaded once, every step
           restores the initial estimates on the device and solves (CUDA
           events inside the library), L2 flushed between steps.
   e2e     through the C ABI with host buffers: load + optimize (structure
           compilation, H2D, solve, D2H of the solution) per step.
+  fp64_plain  the same two measurements of the FP64 plain solve, and the
+          final-cost gap and pose error of the mixed solve against it.
+  config1  the 10-keyframe window: mixed and FP64 plain rates, the serial
+          oracle's rate on it, and the gap.
   cpu_baseline  the oracle (a restatement of the reference's g2o path), one
           thread, on a bounded number of whole solves of the same problem.
 
@@ -34,7 +39,7 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
-LBA_ITERS = 10
+LBA_ITERS = {1: 10, 2: 10, 5: 20}  # LM iterations per configuration
 FP64_NOMINAL_GFLOPS = 1250.0  # FP64 rate of the part (nominal)
 PIVOT_CHAIN_CYCLES = 300      # dependent FP64 FMA (64) + reciprocal seed and cubic Newton step (~237)
 
@@ -45,7 +50,11 @@ def clk_mhz_nominal() -> float:
             return float(json.load(f).get("sm_max_mhz", 2070.0))
     except (OSError, ValueError):
         return 2070.0
-METRIC = "LM edges linearised/s (local BA, 30 KF x 3 cams, 20k points)"
+
+
+def metric_name(pr, iters: int) -> str:
+    return (f"LM edges linearised/s (local BA, {pr.n_poses} KF x 3 cams, {pr.n_points // 1000}k points, "
+            f"{iters} LM iterations)")
 
 
 def parse():
@@ -56,6 +65,10 @@ def parse():
     ap.add_argument("--impl", default="mcba", choices=["mcba", "reference"])
     ap.add_argument("--config", type=int, default=2, choices=[1, 2, 4, 5])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--iters", type=int, default=None,
+                    help="LM iterations per solve (default: 10 for configs 1 and 2, 20 for config 5)")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="skip the FP64-plain comparison and the config-1 block")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -172,20 +185,24 @@ def read_traffic(kernel: str):
 
 
 # --------------------------------------------------------------------- arms --
-def cpu_baseline(pr, seconds: float) -> dict:
+def iters_of(args) -> int:
+    return args.iters if args.iters is not None else LBA_ITERS.get(args.config, 10)
+
+
+def cpu_baseline(pr, seconds: float, iters: int) -> dict:
     from oracle import oracle
 
     t0 = time.perf_counter()
     runs, edges = 0, 0
     while True:
-        r = oracle.optimize(pr, LBA_ITERS, n_threads=1, log_cap=1)
+        r = oracle.optimize(pr, iters, n_threads=1, log_cap=1)
         runs += 1
         edges += r["n_active_edges"] * max(r["iterations_done"], 0)
         if time.perf_counter() - t0 >= seconds or runs >= 50:
             break
     dt = time.perf_counter() - t0
     return {"value": edges / dt, "unit": "edges/s", "cores": 1, "kind": "port",
-            "sample": f"{runs} whole {LBA_ITERS}-iteration solves of the same problem, serial oracle, {dt:.1f} s"}
+            "sample": f"{runs} whole {iters}-iteration solves of the same problem, serial oracle, {dt:.1f} s"}
 
 
 def run_reference(args):
@@ -196,11 +213,12 @@ def run_reference(args):
     from oracle import oracle
 
     pr = synth.config(args.config)
+    iters = iters_of(args)
     threads = os.cpu_count() or 1
     times, edges = [], 0
     for i in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        r = oracle.optimize(pr, LBA_ITERS, n_threads=threads, log_cap=1)
+        r = oracle.optimize(pr, iters, n_threads=threads, log_cap=1)
         dt = time.perf_counter() - t0
         if i >= args.warmup:
             times.append(dt)
@@ -208,11 +226,11 @@ def run_reference(args):
     ms = 1e3 * statistics.mean(times)
     value = edges / (ms / 1e3)
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": args.gpus,
+        "impl": "reference", "metric": metric_name(pr, iters), "value": value, "unit": "edges/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
         "config": {"workload": pr.name, "edges": pr.n_edges, "keyframes": pr.n_poses, "points": pr.n_points,
-                   "lm_iterations": LBA_ITERS, "solver": "oracle restatement of g2o LM + Schur, OpenMP"},
+                   "lm_iterations": iters, "solver": "oracle restatement of g2o LM + Schur, OpenMP"},
         "cpu_baseline": {"value": value, "unit": "edges/s", "cores": threads, "kind": "port",
                          "sample": f"{args.steps} whole solves after {args.warmup} warm-up"},
         "e2e": {"value": value, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -253,6 +271,96 @@ def run_knn_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def _device_leg(ba, pr, precision, iters, steps, warmup, flush, local):
+    """Device-resident solves (problem uploaded once, initial estimates
+    restored on the device each step, L2 flushed before each): the open
+    solver, per-step device ms, kernel launches and the last stats."""
+    import torch
+
+    s = ba.Solver(precision=precision, device=local, use_graph=True)
+    s.load(pr)
+    s.prepare()
+    for _ in range(warmup):
+        s.solve_prepared(iters)
+    step_ms, launches, st = [], 0, None
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        st = s.solve_prepared(iters)
+        step_ms.append(st["ms_total"])
+        launches += st["kernel_launches"]
+    return s, step_ms, launches, st
+
+
+def _e2e_leg(ba, pr, precision, iters, steps, warmup, local, world):
+    """The same solve through the C ABI with host buffers: create, load
+    (structure compilation, H2D), optimize, read the estimates back, destroy."""
+    import torch
+
+    e2e_ms, h2d, d2h, st2 = [], 0, 0, None
+    for i in range(warmup + steps):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        with ba.Solver(precision=precision, device=local) as s2:
+            s2.load(pr)
+            st2 = s2.optimize(iters)
+            s2.state()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t1
+        if i >= warmup:
+            e2e_ms.append(1e3 * dt)
+            h2d, d2h = st2["h2d_bytes"], st2["d2h_bytes"]
+    return {"value": world * st2["edges_linearized"] / (statistics.mean(e2e_ms) / 1e3), "unit": "edges/s",
+            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": statistics.mean(e2e_ms)}
+
+
+def _fp64_cost(ba, pr, qt, X, local) -> float:
+    """activeRobustChi2 of the estimates (qt, X), evaluated in FP64."""
+    with ba.Solver(precision="fp64", device=local) as s:
+        s.load(pr)
+        s.set_state(qt, X)
+        return s.optimize(0)["initial_chi2"]
+
+
+def _rot_err(qa, qb) -> float:
+    va, vb = np.asarray(qa[:3]), np.asarray(qb[:3])
+    w = qa[3] * qb[3] + va @ vb
+    v = qb[3] * va - qa[3] * vb - np.cross(va, vb)
+    return float(2 * np.arctan2(np.linalg.norm(v), abs(w)))
+
+
+def _gap(ba, pr, mixed_state, plain_state, plain_chi, local) -> dict:
+    """Final-cost gap of the mixed solve (its estimates costed in FP64) and its
+    largest pose difference, against the FP64 plain solve."""
+    chi_m = _fp64_cost(ba, pr, mixed_state[0], mixed_state[1], local)
+    qm, qp = mixed_state[0], plain_state[0]
+    return {"final_cost_rel": (chi_m - plain_chi) / plain_chi, "bound": 1e-6,
+            "within_bound": bool(abs(chi_m - plain_chi) <= 1e-6 * plain_chi),
+            "mixed_final_chi2_fp64": chi_m, "fp64_final_chi2": plain_chi,
+            "max_pose_err_m": float(np.abs(qm[:, 4:] - qp[:, 4:]).max()),
+            "max_pose_err_rad": max(_rot_err(qm[k, :4], qp[k, :4]) for k in range(len(qm)))}
+
+
+def _compare(ba, pr, iters, steps, warmup, flush, local, world, with_e2e: bool) -> dict:
+    """Mixed and FP64 plain on one problem: device-resident rates, optional
+    end-to-end rates, and the gap."""
+    out = {}
+    states = {}
+    for prec in ("mixed", "fp64"):
+        s, ms, _, st = _device_leg(ba, pr, prec, iters, steps, warmup, flush, local)
+        s.fetch_state()
+        states[prec] = s.state()
+        s.close()
+        m = statistics.mean(ms)
+        out[prec] = {"value": world * st["edges_linearized"] / (m / 1e3), "unit": "edges/s", "ms_per_step": m,
+                     "final_chi2": st["final_chi2"], "lm_trials": st["trials"]}
+        if with_e2e:
+            out[prec]["e2e"] = _e2e_leg(ba, pr, prec, iters, steps, warmup, local, world)
+    out["gap"] = _gap(ba, pr, states["mixed"], states["fp64"], out["fp64"]["final_chi2"], local)
+    out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    return out
+
+
 def run_mcba(args):
     import torch
 
@@ -273,6 +381,7 @@ def run_mcba(args):
         torch.cuda.synchronize()
 
     pr = synth.config(args.config)
+    iters = iters_of(args)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
 
     # device-resident leg: the LM loop runs as one CUDA graph per solve
@@ -280,7 +389,7 @@ def run_mcba(args):
     s.load(pr)
     s.prepare()
     for _ in range(args.warmup):
-        s.solve_prepared(LBA_ITERS)
+        s.solve_prepared(iters)
     clocks = ClockSampler(local)
     step_ms, launches, stats = [], 0, []
     barrier()
@@ -289,7 +398,7 @@ def run_mcba(args):
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
-        st = s.solve_prepared(LBA_ITERS)
+        st = s.solve_prepared(iters)
         step_ms.append(st["ms_total"])
         launches += st["kernel_launches"]
         stats.append(st)
@@ -297,6 +406,8 @@ def run_mcba(args):
     wall = time.perf_counter() - t0
     clk = clocks.stop()
     st0 = stats[-1]
+    s.fetch_state()
+    state_main = s.state()
     edges_per_step = st0["edges_linearized"]
     ms = statistics.mean(step_ms)
     t_max = ms
@@ -311,14 +422,14 @@ def run_mcba(args):
     sp = ba.Solver(precision=args.precision, device=local, profile=True)
     sp.load(pr)
     sp.prepare()
-    sp.solve_prepared(LBA_ITERS)
+    sp.solve_prepared(iters)
     phase_ms = np.zeros(8)
     phase_n = np.zeros(8, np.int64)
     prof_ms = []
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
-        stp = sp.solve_prepared(LBA_ITERS)
+        stp = sp.solve_prepared(iters)
         phase_ms += np.array(stp["ms_phase"])
         phase_n += np.array(stp["n_phase"])
         prof_ms.append(stp["ms_total"])
@@ -334,14 +445,15 @@ def run_mcba(args):
                 "frac": achieved / peak, "peak_source": peak_kind, "traffic": read_traffic("k_linearize"),
                 "algorithmic_bytes_per_launch": alg, "ms_per_launch": lin_ms,
                 "timing": "CUDA events around each launch, host-driven profiled pass of the same solves"}
-    # the kernel with the largest share of the solve: the FP64 LDL^T of the
-    # reduced camera system, bound by its pivot chain, not by a throughput
+    # the kernel with the largest share of the solve: the FP64 factorisation of
+    # the reduced camera system, bound by its pivot chain, not by a throughput
     chol_ms = phase_ms[5] / max(phase_n[5], 1)
     nred = 6 * int(st0["n_free_poses"])
     flops = nred ** 3 / 3.0 + 4.0 * nred ** 2
     fp64_peak = FP64_NOMINAL_GFLOPS
     roofline_dominant = {
-        "kernel": "k_ldlt_cluster", "bound": "fp64 latency chain", "achieved": flops / (chol_ms / 1e3) / 1e9,
+        "kernel": "k_ldlt_cluster" if nred <= 384 else "k_chol_* (tiled)", "bound": "fp64 latency chain",
+        "achieved": flops / (chol_ms / 1e3) / 1e9,
         "peak": fp64_peak, "unit": "GFLOP/s", "frac": flops / (chol_ms / 1e3) / 1e9 / fp64_peak,
         "peak_source": "nominal FP64 rate of the part (no measured FP64 figure in MEASURED_PEAKS.json)",
         "ms_per_launch": chol_ms, "n": nred,
@@ -352,40 +464,52 @@ def run_mcba(args):
     # end-to-end leg through the C ABI with host buffers
     e2e = None
     if not args.no_e2e:
-        e2e_ms, h2d, d2h = [], 0, 0
-        for i in range(args.warmup + args.steps):
-            torch.cuda.synchronize()
-            t1 = time.perf_counter()
-            with ba.Solver(precision=args.precision, device=local) as s2:
-                s2.load(pr)
-                st2 = s2.optimize(LBA_ITERS)
-                qt, X = s2.state()
-            torch.cuda.synchronize()
-            dt = time.perf_counter() - t1
-            if i >= args.warmup:
-                e2e_ms.append(1e3 * dt)
-                h2d, d2h = st2["h2d_bytes"], st2["d2h_bytes"]
-        e2e = {"value": world * st2["edges_linearized"] / (statistics.mean(e2e_ms) / 1e3), "unit": "edges/s",
-               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-               "ms_per_step": statistics.mean(e2e_ms)}
+        e2e = _e2e_leg(ba, pr, args.precision, iters, args.steps, args.warmup, local, world)
 
-    cpu = None
+    # FP64 plain beside the mixed solve: rates and the final-cost gap
+    fp64_plain = gap = cfg1 = None
+    if args.precision == "mixed" and not args.no_compare:
+        sf, fms, _, stf = _device_leg(ba, pr, "fp64", iters, args.steps, args.warmup, flush, local)
+        sf.fetch_state()
+        state_fp64 = sf.state()
+        sf.close()
+        fm = statistics.mean(fms)
+        fp64_plain = {"value": world * stf["edges_linearized"] / (fm / 1e3), "unit": "edges/s", "ms_per_step": fm,
+                      "final_chi2": stf["final_chi2"], "lm_trials": stf["trials"]}
+        if not args.no_e2e:
+            fp64_plain["e2e"] = _e2e_leg(ba, pr, "fp64", iters, args.steps, args.warmup, local, world)
+        gap = _gap(ba, pr, state_main, state_fp64, stf["final_chi2"], local)
+        if args.config == 2:
+            # the 10-keyframe window the speed-up target is stated on
+            p1 = synth.config(1)
+            cfg1 = {"workload": p1.name, "edges": p1.n_edges, "lm_iterations": LBA_ITERS[1]}
+            cfg1.update(_compare(ba, p1, LBA_ITERS[1], args.steps, args.warmup, flush, local, world, True))
+
+    cpu = cpu1 = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(pr, args.cpu_seconds)
+        cpu = cpu_baseline(pr, args.cpu_seconds, iters)
+        if cfg1 is not None:
+            cpu1 = cpu_baseline(synth.config(1), min(args.cpu_seconds, 4.0), LBA_ITERS[1])
+            cfg1["cpu_baseline"] = cpu1
+            cfg1["mixed_over_cpu_serial"] = cfg1["mixed"]["value"] / cpu1["value"]
+            cfg1["mixed_e2e_over_cpu_serial"] = cfg1["mixed"]["e2e"]["value"] / cpu1["value"]
+            cfg1["target"] = ("mixed >= 20x the serial CPU restatement's edges/s, faster than FP64 plain, "
+                              "final-cost gap <= 1e-6")
 
     if rank == 0:
         line = {
-            "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64",
+            "metric": metric_name(pr, iters), "value": value, "unit": "edges/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64",
             "data": "synthetic (seeded generator with the benchmark's shapes and noise model)",
             "config": {"workload": pr.name, "edges": pr.n_edges, "active_edges": st0["n_active_edges"],
                        "keyframes": pr.n_poses, "free_keyframes": st0["n_free_poses"], "points": pr.n_points,
-                       "lm_iterations": LBA_ITERS, "precision": args.precision,
-                       "l2": "flushed (256 MB write) before every step; working set ~30 MB < L2",
+                       "lm_iterations": iters, "precision": args.precision,
+                       "l2": "flushed (256 MB write) before every step",
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "ba_solve_ms": ms, "final_chi2": st0["final_chi2"], "lm_trials": st0["trials"]},
-            "e2e": e2e, "cpu_baseline": cpu, "roofline": roofline, "roofline_dominant": roofline_dominant,
+            "e2e": e2e, "fp64_plain": fp64_plain, "precision_gap": gap, "config1": cfg1,
+            "cpu_baseline": cpu, "roofline": roofline, "roofline_dominant": roofline_dominant,
             "phases": phases,
             "profiled_ms_per_step": statistics.mean(prof_ms),
             "clocks": clk, "gpu_launches": int(launches), "wall_s_timed_region": wall,
@@ -414,13 +538,13 @@ def run_config4(args):
     clocks = ClockSampler(local)
     with ba.LocalBABatch(wins, precision="mixed", device=local) as b:
         for _ in range(args.warmup):
-            b.solve(LBA_ITERS)
+            b.solve(LBA_ITERS[2])
         wms, edges = [], 0
         clocks.start()
         for _ in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()
-            stats, ms = b.solve(LBA_ITERS)
+            stats, ms = b.solve(LBA_ITERS[2])
             wms.append(ms)
             edges = sum(st["edges_linearized"] for st in stats)
         for _ in range(args.warmup):
@@ -439,7 +563,7 @@ def run_config4(args):
         t0 = time.perf_counter()
         e_cpu = 0
         for pr in wins[:3]:
-            r = oracle.optimize(pr, LBA_ITERS, n_threads=1, log_cap=1)
+            r = oracle.optimize(pr, LBA_ITERS[2], n_threads=1, log_cap=1)
             e_cpu += r["n_active_edges"] * max(r["iterations_done"], 0)
         dt = time.perf_counter() - t0
         cpu = {"value": e_cpu / dt, "unit": "edges/s", "cores": 1, "kind": "port",
@@ -451,7 +575,7 @@ def run_config4(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic (seeded generator with the benchmark's shapes and noise model)",
             "config": {"workload": "config4_batched", "windows": len(wins),
-                       "window_edges": int(sum(w.n_edges for w in wins)), "lm_iterations": LBA_ITERS,
+                       "window_edges": int(sum(w.n_edges for w in wins)), "lm_iterations": LBA_ITERS[2],
                        "pose_only_frames": len(frames), "pose_only_edges": int(sum(f.n_edges for f in frames)),
                        "pose_only_ms": p_ms, "pose_only_frames_per_s": len(frames) / (p_ms / 1e3),
                        "l2": "flushed (256 MB write) before every step"},

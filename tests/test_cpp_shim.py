@@ -24,3 +24,74 @@ def test_shim_builds_and_runs_host_side(tmp_path):
     out = subprocess.run([exe], capture_output=True, text=True)
     assert out.returncode == 0, (out.returncode, out.stdout, out.stderr)
     assert "shim ok" in out.stdout
+
+
+def _write_problem(path, pr, iters, thr):
+    import numpy as np
+
+    with open(path, "wb") as f:
+        np.array([pr.n_cams, pr.n_poses, pr.n_points, pr.n_edges, iters], np.int32).tofile(f)
+        np.array([thr], np.float32).tofile(f)
+        for c in range(pr.n_cams):
+            np.asarray(pr.cam_K[c], np.float32).tofile(f)
+            np.array([pr.cam_bf[c]], np.float32).tofile(f)
+            np.asarray(pr.cam_Tcb[c], np.float32).reshape(16).tofile(f)
+        for i in range(pr.n_poses):
+            np.asarray(pr.pose_Tcw[i], np.float32).reshape(16).tofile(f)
+            np.array([pr.pose_fixed[i]], np.uint8).tofile(f)
+        for i in range(pr.n_points):
+            np.asarray(pr.point_Xw[i], np.float32).tofile(f)
+            np.array([pr.point_fixed[i]], np.uint8).tofile(f)
+        rec = np.dtype([("type", np.uint8), ("pose", np.int32), ("point", np.int32), ("cam", np.int32),
+                        ("obs", np.float32, 3), ("info", np.float32)], align=False)
+        e = np.zeros(pr.n_edges, rec)
+        e["type"], e["pose"], e["point"], e["cam"] = pr.edge_type, pr.edge_pose, pr.edge_point, pr.edge_cam
+        e["obs"] = np.asarray(pr.edge_obs, np.float32).reshape(pr.n_edges, -1)[:, :3]
+        e["info"] = pr.edge_info
+        e.tofile(f)
+
+
+@pytest.mark.gpu
+def test_shim_local_ba_end_to_end_matches_oracle(tmp_path, gpu):
+    """BoundleAdjustment through the C++ shim on the GPU (add vertices and edges
+    one by one, optimize(10), filter with the chi2 callback, recovery_all)
+    against the oracle's local BA: return value, written flag, edge levels and
+    the recovered float estimates."""
+    import numpy as np
+
+    from mcvslam_gb300 import synth
+    from oracle import oracle
+
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    pr = synth.config(1)
+    # the shim's Huber thresholds: sqrt(5.99) for left-camera mono edges,
+    # sqrt(7.815) for the others (include/BAoptimizer.hpp:62-63)
+    pr.edge_delta = np.where(pr.edge_cam == 0, np.float32(2.44744754), np.float32(2.79553223)).astype(np.float32)
+    pr.edge_info = np.ones(pr.n_edges, np.float32)
+    pr.edge_robust = np.ones(pr.n_edges, np.uint8)
+    pr.edge_level = np.zeros(pr.n_edges, np.uint8)
+    N.lib()
+    libdir = os.path.dirname(N.LIB_PATH)
+    exe = str(tmp_path / "shim_lba")
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "shim_lba.cpp"), "-L", libdir, "-lmcba",
+                    "-Wl,-rpath," + libdir, "-o", exe], check=True)
+    inp, outp = str(tmp_path / "p.bin"), str(tmp_path / "o.bin")
+    _write_problem(inp, pr, 10, 5.991)
+    run = subprocess.run([exe, inp, outp], capture_output=True, text=True)
+    assert run.returncode == 0, (run.returncode, run.stdout, run.stderr)
+    raw = open(outp, "rb").read()
+    head = np.frombuffer(raw[:12], np.int32)
+    off = 12
+    levels = np.frombuffer(raw[off:off + pr.n_edges], np.uint8)
+    off += pr.n_edges
+    T = np.frombuffer(raw[off:off + 64 * pr.n_poses], np.float32).reshape(pr.n_poses, 16)
+    off += 64 * pr.n_poses
+    X = np.frombuffer(raw[off:off + 12 * pr.n_points], np.float32).reshape(pr.n_points, 3)
+    o = oracle.local_ba(pr, 10, 5.991)
+    assert head[2] == 0, head
+    assert head[0] == o["ret"] and head[1] == o["written"]
+    np.testing.assert_array_equal(levels, o["edge_level"])
+    np.testing.assert_allclose(T, o["pose_Tcw"].reshape(pr.n_poses, 16), rtol=0, atol=2e-5)
+    np.testing.assert_allclose(X, o["point_X"].astype(np.float32), rtol=0, atol=1e-4)
