@@ -265,6 +265,63 @@ int mcba_pose_optimization(mcba_problem* p, int32_t rounds, int32_t iterations, 
 int mcba_local_ba(mcba_problem* p, int32_t iterations, float chi2_threshold, int32_t* success_edges,
                   int32_t* written);
 
+/* ------------------------------------------- local-BA window of a map -- */
+/* Flat tables of a SLAM map, as Map::AddKeyFrame reads them before its local
+ * BA (src/Map.cpp:140-145): keyframes with the map points their LEFT (0) and
+ * WIDE (1) objects observe, map points with the keyframes bound to them
+ * (MapPoint::GetAllKeyFrame), the essential graph, and the rig.  Host arrays.
+ * Each (keyframe, object, map point) appears at most once, as in an Object.
+ * Frame ids must lie in [0, 2^39) and n_keyframes below 2^24. */
+typedef struct mcba_map_desc {
+  int32_t n_keyframes;
+  const int64_t* kf_id;        /* [K] Frame::id */
+  const float* kf_Tcw;         /* [K][16] T_body_world, row-major (Frame::GetPose) */
+  const int32_t* obs_begin;    /* [K + 1] observations of each keyframe */
+  const int32_t* obs_point;    /* [O] map point */
+  const uint8_t* obs_object;   /* [O] 0 LEFT, 1 WIDE */
+  const float* obs_uv;         /* [O][2] keypoint position */
+  const float* obs_ur;         /* [O] u_right of a LEFT keypoint, -1 when none */
+  const uint8_t* obs_octave;   /* [O] keypoint octave */
+  int32_t n_points;
+  const float* mp_Xw;          /* [P][3] MapPoint::GetWorldPos */
+  const int32_t* mp_kf_begin;  /* [P + 1] keyframes bound to each map point */
+  const int32_t* mp_kf;
+  const int32_t* ess_begin;    /* [K + 1] essential-graph neighbours */
+  const int32_t* ess_adj;
+  int32_t n_levels;
+  const float* inv_sigma2_left;  /* [n_levels] mvInvLevelSigma2 of the left extractor */
+  const float* inv_sigma2_wide;  /* [n_levels] of the wide extractor */
+  float K_left[4];             /* fx fy cx cy of the LEFT camera (T_cam_body = I) */
+  float K_wide[4];             /* of the WIDE camera */
+  float T_wide_body[16];       /* T_cam_body of the WIDE camera (kf->Twl) */
+  float bf;                    /* stereo baseline x fx (kf->bf) */
+} mcba_map_desc;
+
+typedef struct mcba_window_info {
+  int32_t n_local;         /* keyframes optimised, the new one included */
+  int32_t n_anchor;        /* fixed anchor keyframes */
+  int32_t n_poses, n_points, n_fixed_points, n_edges;
+} mcba_window_info;
+
+/* The local BA set-up of Map::AddKeyFrame for keyframe `cur` on the GPU
+ * (src/Map.cpp:142-145): GrabLocalMap_Mappoint(cur, hop) (src/Map.cpp:730-756),
+ * GrabAnchorKeyFrames (src/Map.cpp:775-796), cur added, then the vertex and
+ * edge insertion of PoseEstimation::BoundleAdjustment
+ * (include/PoseEstimation.hpp:36-97) with ThisMapPointBeFix per map point
+ * (src/PoseEstimation.cpp:153-163) -- replacing its hash-set walks and per-edge
+ * allocations.  The problem is loaded into p (camera 0 LEFT, camera 1 WIDE):
+ * poses are the anchors then the window keyframes in ascending map index,
+ * points in order of first edge, edges in the insertion loop's order (each
+ * keyframe's LEFT observations, then its WIDE ones, in table order).  Then
+ * mcba_local_ba(p, 10, 5.991, ...) is BoundleAdjustment's optimise and
+ * filter.  Outputs (each may be NULL): kf_role [K] (bit 0 optimised, bit 1
+ * anchor), pose_kf [<= K] map keyframe of each pose, point_mp [<= P] map
+ * point of each point, point_fixed [<= P] ThisMapPointBeFix.
+ * Errors: MCBA_ERR_INVALID for bad arguments or tables (an index or CSR range
+ * out of bounds). */
+int mcba_local_window(mcba_problem* p, const mcba_map_desc* map, int32_t cur, int32_t hop, uint8_t* kf_role,
+                      int32_t* pose_kf, int32_t* point_mp, uint8_t* point_fixed, mcba_window_info* info);
+
 /* ---------------------------------------------- Hamming k = 2 matching -- */
 /* Matcher::KnnMatch over descriptor lists (src/Matcher.cpp:245-302): for
  * each of nq 32-byte query descriptors, the best and second-best of nt train

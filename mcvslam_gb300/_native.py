@@ -98,6 +98,25 @@ class StereoBatchDesc(ctypes.Structure):
     ]
 
 
+class MapDesc(ctypes.Structure):
+    """mcba_map_desc (host arrays)."""
+    _fields_ = [
+        ("n_keyframes", ctypes.c_int32), ("kf_id", ctypes.c_void_p), ("kf_Tcw", ctypes.c_void_p),
+        ("obs_begin", ctypes.c_void_p), ("obs_point", ctypes.c_void_p), ("obs_object", ctypes.c_void_p),
+        ("obs_uv", ctypes.c_void_p), ("obs_ur", ctypes.c_void_p), ("obs_octave", ctypes.c_void_p),
+        ("n_points", ctypes.c_int32), ("mp_Xw", ctypes.c_void_p), ("mp_kf_begin", ctypes.c_void_p),
+        ("mp_kf", ctypes.c_void_p), ("ess_begin", ctypes.c_void_p), ("ess_adj", ctypes.c_void_p),
+        ("n_levels", ctypes.c_int32), ("inv_sigma2_left", ctypes.c_void_p), ("inv_sigma2_wide", ctypes.c_void_p),
+        ("K_left", ctypes.c_float * 4), ("K_wide", ctypes.c_float * 4), ("T_wide_body", ctypes.c_float * 16),
+        ("bf", ctypes.c_float),
+    ]
+
+
+class WindowInfo(ctypes.Structure):
+    _fields_ = [("n_local", ctypes.c_int32), ("n_anchor", ctypes.c_int32), ("n_poses", ctypes.c_int32),
+                ("n_points", ctypes.c_int32), ("n_fixed_points", ctypes.c_int32), ("n_edges", ctypes.c_int32)]
+
+
 _LIB = None
 
 
@@ -148,6 +167,8 @@ def _declare(L):
         "mcba_dump_hessian": ([P, ctypes.c_char_p], ctypes.c_int),
         "mcba_pose_optimization": ([P, i32, i32, ctypes.c_float, i32, c_i32_p, c_i32_p], ctypes.c_int),
         "mcba_local_ba": ([P, i32, ctypes.c_float, c_i32_p, c_i32_p], ctypes.c_int),
+        "mcba_local_window": ([P, ctypes.POINTER(MapDesc), i32, i32, c_u8_p, c_i32_p, c_i32_p, c_u8_p,
+                               ctypes.POINTER(WindowInfo)], ctypes.c_int),
         "mcba_reproj_forward": ([i32, ctypes.c_int64, P, P, P, P, P, P, P, P, P], ctypes.c_int),
         "mcba_reproj_backward": ([i32, ctypes.c_int64, P, P, P, P, P, P, P, P, P, P, P, P, P, P], ctypes.c_int),
         "mcba_batch_pose_only": ([i32, i32, i32, c_i32_p, i32, c_float_p, c_float_p, c_i32_p, c_float_p, c_float_p,

@@ -185,6 +185,55 @@ class Solver:
         N.check(self.L.mcba_local_ba(self.h, iterations, chi2_thr, ctypes.byref(a), ctypes.byref(b)), self.h)
         return a.value, b.value
 
+    def local_window(self, m, cur: int, hop: int = 1) -> dict:
+        """Map::AddKeyFrame's local-BA set-up for keyframe `cur` of the map
+        tables `m` (a synth.MapTables) on the GPU: the window is chosen and its
+        problem loaded into this solver (mcba_local_window).  Returns the roles
+        (bit 0 optimised, bit 1 anchor), the map keyframe of each pose, the map
+        point of each point, ThisMapPointBeFix per point and the counts."""
+        a = {}
+
+        def arr(name, dt):
+            x = np.ascontiguousarray(getattr(m, name), dtype=dt)
+            a[name] = x
+            return x.ctypes.data
+
+        d = N.MapDesc()
+        d.n_keyframes = m.n_keyframes
+        d.kf_id = arr("kf_id", np.int64)
+        d.kf_Tcw = arr("kf_Tcw", np.float32)
+        d.obs_begin = arr("obs_begin", np.int32)
+        d.obs_point = arr("obs_point", np.int32)
+        d.obs_object = arr("obs_object", np.uint8)
+        d.obs_uv = arr("obs_uv", np.float32)
+        d.obs_ur = arr("obs_ur", np.float32)
+        d.obs_octave = arr("obs_octave", np.uint8)
+        d.n_points = m.n_points
+        d.mp_Xw = arr("mp_Xw", np.float32)
+        d.mp_kf_begin = arr("mp_kf_begin", np.int32)
+        d.mp_kf = arr("mp_kf", np.int32)
+        d.ess_begin = arr("ess_begin", np.int32)
+        d.ess_adj = arr("ess_adj", np.int32)
+        d.n_levels = int(len(m.inv_sigma2_left))
+        d.inv_sigma2_left = arr("inv_sigma2_left", np.float32)
+        d.inv_sigma2_wide = arr("inv_sigma2_wide", np.float32)
+        d.K_left[:] = [float(x) for x in m.K_left]
+        d.K_wide[:] = [float(x) for x in m.K_wide]
+        d.T_wide_body[:] = [float(x) for x in np.asarray(m.T_wide_body).reshape(16)]
+        d.bf = float(m.bf)
+        role = np.zeros(m.n_keyframes, np.uint8)
+        pose_kf = np.zeros(m.n_keyframes, np.int32)
+        point_mp = np.zeros(max(m.n_points, 1), np.int32)
+        point_fixed = np.zeros(max(m.n_points, 1), np.uint8)
+        info = N.WindowInfo()
+        N.check(self.L.mcba_local_window(self.h, ctypes.byref(d), cur, hop, _p(role, N.c_u8_p),
+                                         _p(pose_kf, N.c_i32_p), _p(point_mp, N.c_i32_p), _p(point_fixed, N.c_u8_p),
+                                         ctypes.byref(info)), self.h)
+        self.n_poses, self.n_points, self.n_edges = info.n_poses, info.n_points, info.n_edges
+        return {"kf_role": role, "pose_kf": pose_kf[:info.n_poses], "point_mp": point_mp[:info.n_points],
+                "point_fixed": point_fixed[:info.n_points], "n_local": info.n_local, "n_anchor": info.n_anchor,
+                "n_fixed_points": info.n_fixed_points, "n_edges": info.n_edges}
+
     def dump_hessian(self, path: str) -> None:
         N.check(self.L.mcba_dump_hessian(self.h, path.encode()), self.h)
 

@@ -21,6 +21,7 @@
 #include "mcba.h"
 #include "mcba_host_pool.h"
 #include "mcba_internal.h"
+#include "mcba_window.h"
 
 namespace mcba {
 namespace {
@@ -416,6 +417,7 @@ const char* mcba_status_string(int s) {
 
 int mcba_release_cached(int32_t device) {
   mcba::solver_release_cached(device);
+  mcba::window_release(device);
   return MCBA_OK;
 }
 
@@ -1079,6 +1081,84 @@ int mcba_pose_optimization(mcba_problem* p, int32_t rounds, int32_t iters, float
 }
 
 // include/PoseEstimation.hpp:104-118 with src/PoseEstimation.cpp:132-151
+int mcba_local_window(mcba_problem* p, const mcba_map_desc* m, int32_t cur, int32_t hop, uint8_t* kf_role,
+                      int32_t* pose_kf, int32_t* point_mp, uint8_t* point_fixed, mcba_window_info* info) {
+  if (!p || !m) return fail(p, MCBA_ERR_INVALID, "null argument");
+  const int K = m->n_keyframes, P = m->n_points;
+  if (K <= 0 || K >= (1 << 24) || P < 0 || hop < 1 || cur < 0 || cur >= K || m->n_levels <= 0)
+    return fail(p, MCBA_ERR_INVALID, "bad window arguments");
+  if (!m->kf_id || !m->kf_Tcw || !m->obs_begin || !m->mp_kf_begin || !m->ess_begin || !m->inv_sigma2_left ||
+      !m->inv_sigma2_wide || (P && !m->mp_Xw))
+    return fail(p, MCBA_ERR_INVALID, "null map table");
+  const int32_t O = m->obs_begin[K], B = m->mp_kf_begin[P], A = m->ess_begin[K];
+  if (O >= (1 << 29)) return fail(p, MCBA_ERR_TOO_LARGE, "more than 2^29 observations");
+  if (m->obs_begin[0] != 0 || m->mp_kf_begin[0] != 0 || m->ess_begin[0] != 0 || O < 0 || B < 0 || A < 0 ||
+      m->obs_begin[cur] < 0 || m->obs_begin[cur + 1] < m->obs_begin[cur] || m->obs_begin[cur + 1] > O)
+    return fail(p, MCBA_ERR_INVALID, "bad CSR table bounds");
+  if ((O && (!m->obs_point || !m->obs_object || !m->obs_uv || !m->obs_ur || !m->obs_octave)) ||
+      (B && !m->mp_kf) || (A && !m->ess_adj))
+    return fail(p, MCBA_ERR_INVALID, "null map table");
+  for (int k = 0; k < K; ++k)
+    if (m->kf_id[k] < 0 || m->kf_id[k] >= (int64_t(1) << 39)) return fail(p, MCBA_ERR_INVALID, "keyframe id out of range");
+  // monotone offsets: the ranges are disjoint, so the window has at most 2 O
+  // edges (a keyframe is an anchor, a window member or both)
+  for (int k = 0; k < K; ++k)
+    if (m->obs_begin[k + 1] < m->obs_begin[k] || m->ess_begin[k + 1] < m->ess_begin[k])
+      return fail(p, MCBA_ERR_INVALID, "CSR offsets not monotone");
+  for (int i = 0; i < P; ++i)
+    if (m->mp_kf_begin[i + 1] < m->mp_kf_begin[i]) return fail(p, MCBA_ERR_INVALID, "CSR offsets not monotone");
+  WindowHost w;
+  std::string e;
+  const int r = window_assemble(p->opt.device, m, cur, hop, w, &e);
+  if (r) return fail(p, r, e);
+  // the problem: camera 0 LEFT (T_cam_body = I, stereo bf), camera 1 WIDE
+  const float I4[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+  float camK[8], camT[32];
+  const float camB[2] = {m->bf, 0.f};
+  std::memcpy(camK, m->K_left, sizeof(float) * 4);
+  std::memcpy(camK + 4, m->K_wide, sizeof(float) * 4);
+  std::memcpy(camT, I4, sizeof(I4));
+  std::memcpy(camT + 16, m->T_wide_body, sizeof(float) * 16);
+  const int NPo = (int)w.pose_kf.size(), NPt = (int)w.point_mp.size(), E = (int)w.e_type.size();
+  std::vector<float> T((size_t)NPo * 16), X((size_t)NPt * 3);
+  for (int i = 0; i < NPo; ++i) std::memcpy(&T[16 * (size_t)i], m->kf_Tcw + 16 * (size_t)w.pose_kf[i], 64);
+  for (int i = 0; i < NPt; ++i) std::memcpy(&X[3 * (size_t)i], m->mp_Xw + 3 * (size_t)w.point_mp[i], 12);
+  mcba_problem_desc d{};
+  d.n_cams = 2;
+  d.cam_K = camK;
+  d.cam_bf = camB;
+  d.cam_Tcb = camT;
+  d.n_poses = NPo;
+  d.pose_Tcw = T.data();
+  d.pose_fixed = w.pose_fixed.data();
+  d.n_points = NPt;
+  d.point_Xw = X.data();
+  d.point_fixed = w.point_fixed.data();
+  d.n_edges = E;
+  d.edge_type = w.e_type.data();
+  d.edge_pose = w.e_pose.data();
+  d.edge_point = w.e_point.data();
+  d.edge_cam = w.e_cam.data();
+  d.edge_obs = w.e_obs.data();
+  d.edge_info = w.e_info.data();
+  d.edge_delta = w.e_delta.data();
+  const int rl = mcba_load(p, &d);
+  if (rl) return rl;
+  if (kf_role) std::memcpy(kf_role, w.kf_role.data(), (size_t)K);
+  if (pose_kf && NPo) std::memcpy(pose_kf, w.pose_kf.data(), sizeof(int32_t) * NPo);
+  if (point_mp && NPt) std::memcpy(point_mp, w.point_mp.data(), sizeof(int32_t) * NPt);
+  if (point_fixed && NPt) std::memcpy(point_fixed, w.point_fixed.data(), (size_t)NPt);
+  if (info) {
+    info->n_local = w.n_local;
+    info->n_anchor = w.n_anchor;
+    info->n_poses = NPo;
+    info->n_points = NPt;
+    info->n_fixed_points = w.n_fixed_points;
+    info->n_edges = E;
+  }
+  return MCBA_OK;
+}
+
 int mcba_local_ba(mcba_problem* p, int32_t iters, float thr, int32_t* success, int32_t* written) {
   if (!p || iters < 0) return fail(p, MCBA_ERR_INVALID, "bad argument");
   int r = mcba_optimize(p, iters, nullptr);

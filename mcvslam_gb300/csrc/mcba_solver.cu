@@ -421,16 +421,18 @@ __device__ __forceinline__ void pose_reduce_warp(const Bufs& B, int Kf, int i, i
 }
 
 // Hll / b_l: sum over the (<= a few) edges of each free point.
-// Hll is summed in FP64 (from the float-float pairs of FP32 rows), b_l in
-// the linearisation type.
+// Hll is stored in FP64: FP32 rows sum their float-float pairs with TwoSum
+// (Acc<float>: the high parts exactly, the low parts and the TwoSum errors in
+// a second float) and convert once per point; b_l stays in the linearisation
+// type.
 template <typename R>
 __device__ __forceinline__ void point_reduce_thread(const Bufs& B, int Lf, int l) {
   if (l >= Lf) return;
   const int e0 = B.pt_begin[l], e1 = B.pt_begin[l + 1];
-  double h[6];
+  Acc<R> h[6];
   R s[3];
 #pragma unroll
-  for (int k = 0; k < 6; ++k) h[k] = 0.0;
+  for (int k = 0; k < 6; ++k) h[k].zero();
 #pragma unroll
   for (int k = 0; k < 3; ++k) s[k] = R(0);
 #pragma unroll 4
@@ -438,15 +440,15 @@ __device__ __forceinline__ void point_reduce_thread(const Bufs& B, int Lf, int l
     const R* row = Ptrs<R>::p(B.rows) + (size_t)e * row_stride<R>();
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
-      h[k] += (double)row[18 + k];
-      if constexpr (row_stride<R>() > kHllLo) h[k] += (double)row[kHllLo + k];
+      h[k].add(row[18 + k]);
+      if constexpr (row_stride<R>() > kHllLo) h[k].lo = __fadd_rn(h[k].lo, row[kHllLo + k]);
     }
 #pragma unroll
     for (int k = 0; k < 3; ++k) s[k] += row[24 + k];
   }
   double* H = B.Hll + (size_t)l * 6;
 #pragma unroll
-  for (int k = 0; k < 6; ++k) H[k] = h[k];
+  for (int k = 0; k < 6; ++k) H[k] = h[k].value();
   R* b = Ptrs<R>::p(B.bl) + 3 * (size_t)l;
 #pragma unroll
   for (int k = 0; k < 3; ++k) b[k] = s[k];

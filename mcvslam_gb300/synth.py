@@ -375,6 +375,131 @@ def reference_style(seed: int, n_kf: int = 5, n_points: int = 300) -> Problem:
     return pr
 
 
+# --------------------------------------------------------------- map tables --
+@dataclasses.dataclass
+class MapTables:
+    """Flat tables of a SLAM map in the layout of mcba_map_desc: what
+    Map::AddKeyFrame reads before its local BA (src/Map.cpp:140-145) --
+    keyframes with their LEFT and WIDE observations, map points with the
+    keyframes bound to them (MapPoint::GetAllKeyFrame), the essential graph."""
+    kf_id: np.ndarray        # int64 [K] Frame::id
+    kf_Tcw: np.ndarray       # float32 [K, 16] T_body_world
+    obs_begin: np.ndarray    # int32 [K + 1]
+    obs_point: np.ndarray    # int32 [O]
+    obs_object: np.ndarray   # uint8 [O] 0 LEFT, 1 WIDE
+    obs_uv: np.ndarray       # float32 [O, 2]
+    obs_ur: np.ndarray       # float32 [O] u_right (-1: none)
+    obs_octave: np.ndarray   # uint8 [O]
+    mp_Xw: np.ndarray        # float32 [P, 3]
+    mp_kf_begin: np.ndarray  # int32 [P + 1]
+    mp_kf: np.ndarray        # int32 [B]
+    ess_begin: np.ndarray    # int32 [K + 1]
+    ess_adj: np.ndarray      # int32 [A]
+    inv_sigma2_left: np.ndarray   # float32 [L]
+    inv_sigma2_wide: np.ndarray   # float32 [L]
+    K_left: np.ndarray       # float32 [4]
+    K_wide: np.ndarray       # float32 [4]
+    T_wide_body: np.ndarray  # float32 [16]
+    bf: float = 0.0
+
+    @property
+    def n_keyframes(self) -> int:
+        return int(self.kf_id.shape[0])
+
+    @property
+    def n_points(self) -> int:
+        return int(self.mp_Xw.shape[0])
+
+
+def map_tables(n_kf: int, n_points: int, seed: int, per_object: int = 300, stereo_frac: float = 0.5,
+               unbound_frac: float = 0.02, n_levels: int = 8, ess_k: int = 4) -> MapTables:
+    """A keyframe map on the reference rig (LEFT = body, WIDE camera, right
+    image through u_right): n_kf keyframes on a drone path, n_points map points
+    around it, at most per_object observations per keyframe and camera.  The
+    last keyframe is the new one: like the reference at its local BA, its
+    observations are not yet bound back to their map points (the binding
+    follows the BA, src/Map.cpp:148-154); a few other bindings are missing at
+    random.  Keyframe ids rise with gaps, the first is 0.  u_right values
+    include some in [0, 1), which the BA treats as mono (MIN_DISPARITY = 1).
+    Essential graph: each keyframe linked to its ess_k most covisible others."""
+    rng = np.random.default_rng(seed)
+    rig = reference_rig()
+    T_wb = drone_trajectory(rng, n_kf)
+    T_bw = inv_T(T_wb)
+    anchor = rng.integers(0, n_kf, n_points)
+    centre = T_wb[anchor, :3, 3] + T_wb[anchor, :3, 2] * 8.0
+    X = centre + rng.uniform(-0.5, 0.5, (n_points, 3)) * np.array([16.0, 8.0, 10.0])
+    cams = (0, 2)  # LEFT, WIDE of the rig
+    ob_kf, ob_pt, ob_obj, ob_uv, ob_ur = [], [], [], [], []
+    for k in range(n_kf):
+        for o, c in enumerate(cams):
+            Tcw = rig.T_cb[c] @ T_bw[k]
+            Pc = X @ Tcw[:3, :3].T + Tcw[:3, 3]
+            ok = Pc[:, 2] > 0.5
+            uv = _project(rig.K[c].astype(np.float64), Pc)
+            w, h = rig.size[c]
+            ok &= (uv[:, 0] >= 0) & (uv[:, 0] < w) & (uv[:, 1] >= 0) & (uv[:, 1] < h)
+            idx = np.nonzero(ok)[0]
+            if len(idx) > per_object:
+                idx = np.sort(rng.choice(idx, per_object, replace=False))
+            idx = rng.permutation(idx)  # table order within an object is arbitrary
+            z = uv[idx] + rng.normal(0, 1.0, (len(idx), 2))
+            ur = np.full(len(idx), -1.0)
+            if o == 0:
+                st = rng.random(len(idx)) < stereo_frac
+                ur[st] = z[st, 0] - rig.bf[0] / Pc[idx[st], 2]
+                small = st & (rng.random(len(idx)) < 0.1)
+                ur[small] = rng.uniform(0.0, 1.0, int(small.sum()))
+            ob_kf.append(np.full(len(idx), k)); ob_pt.append(idx); ob_obj.append(np.full(len(idx), o))
+            ob_uv.append(z); ob_ur.append(ur)
+    kf = np.concatenate(ob_kf); pt = np.concatenate(ob_pt); obj = np.concatenate(ob_obj)
+    uvs = np.concatenate(ob_uv); urs = np.concatenate(ob_ur)
+    # interleave LEFT and WIDE rows inside a keyframe (the table need not be grouped)
+    order = np.lexsort((rng.random(len(kf)), kf))
+    kf, pt, obj, uvs, urs = kf[order], pt[order], obj[order], uvs[order], urs[order]
+    obs_begin = np.zeros(n_kf + 1, np.int32)
+    obs_begin[1:] = np.cumsum(np.bincount(kf, minlength=n_kf))
+    # bindings point -> keyframe (set semantics), minus the new keyframe
+    bound = (kf != n_kf - 1) & (rng.random(len(kf)) >= unbound_frac)
+    pairs = np.unique(np.stack([pt[bound], kf[bound]], 1), axis=0) if bound.any() else np.zeros((0, 2), np.int64)
+    # the binding list of a point in an arbitrary order
+    pairs = pairs[np.lexsort((rng.random(len(pairs)), pairs[:, 0]))]
+    mp_kf_begin = np.zeros(n_points + 1, np.int32)
+    mp_kf_begin[1:] = np.cumsum(np.bincount(pairs[:, 0], minlength=n_points))
+    # essential graph from covisibility
+    M = np.zeros((n_kf, n_points), np.uint8)
+    M[kf, pt] = 1
+    cov = M.astype(np.int32) @ M.T.astype(np.int32)
+    np.fill_diagonal(cov, 0)
+    adj = [set() for _ in range(n_kf)]
+    for k in range(n_kf):
+        best = np.argsort(-cov[k], kind="stable")[:ess_k]
+        for j in best:
+            if cov[k, j] > 0:
+                adj[k].add(int(j)); adj[int(j)].add(k)
+    ess_begin = np.zeros(n_kf + 1, np.int32)
+    ess_adj = []
+    for k in range(n_kf):
+        nb = rng.permutation(sorted(adj[k]))
+        ess_adj.extend(int(x) for x in nb)
+        ess_begin[k + 1] = len(ess_adj)
+    ids = np.concatenate([[0], np.cumsum(rng.integers(1, 4, n_kf - 1))]).astype(np.int64)
+    T_init = T_bw.copy()
+    for k in range(2, n_kf):
+        T_init[k] = _perturb_pose(rng, T_bw[k], 1.0, 0.05)
+    X_init = X + rng.normal(0, 0.1, X.shape)
+    scale = 1.2 ** np.arange(n_levels)
+    inv_s2 = (1.0 / (scale * scale)).astype(np.float32)
+    return MapTables(
+        kf_id=ids, kf_Tcw=T_init.astype(np.float32).reshape(n_kf, 16), obs_begin=obs_begin,
+        obs_point=pt.astype(np.int32), obs_object=obj.astype(np.uint8), obs_uv=uvs.astype(np.float32),
+        obs_ur=urs.astype(np.float32), obs_octave=rng.integers(0, n_levels, len(kf)).astype(np.uint8),
+        mp_Xw=X_init.astype(np.float32), mp_kf_begin=mp_kf_begin, mp_kf=pairs[:, 1].astype(np.int32),
+        ess_begin=ess_begin, ess_adj=np.asarray(ess_adj, np.int32), inv_sigma2_left=inv_s2,
+        inv_sigma2_wide=inv_s2.copy(), K_left=rig.K[0].copy(), K_wide=rig.K[2].copy(),
+        T_wide_body=rig.T_cb[2].astype(np.float32).reshape(16), bf=float(rig.bf[0]))
+
+
 # ---------------------------------------------------------------- pose-only --
 def pose_only(n_obs: int, seed: int, outlier_frac: float = 0.10, rig: Optional[Rig] = None,
               delta=HUBER_BENCH) -> Problem:

@@ -1,6 +1,6 @@
 """Build recipe for the CPU oracle (test infrastructure, not product code).
 
-Compiles oracle/g2o_oracle.cpp and oracle/matcher_oracle.cpp twice into
+Compiles oracle/g2o_oracle.cpp, matcher_oracle.cpp and window_oracle.cpp twice into
 oracle/_build/:
   liboracle.so      serial restatement (the reference's g2o is built with
                     OpenMP off, ThirdParty/g2o/CMakeLists.txt:139-149)
@@ -18,6 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_build")
 SRC = os.path.join(HERE, "g2o_oracle.cpp")
 SRC_MATCH = os.path.join(HERE, "matcher_oracle.cpp")
+SRC_WINDOW = os.path.join(HERE, "window_oracle.cpp")
 HDR = os.path.join(HERE, "g2o_oracle.h")
 
 TARGETS = {
@@ -30,7 +31,7 @@ def _stale(out: str) -> bool:
     if not os.path.exists(out):
         return True
     t = os.path.getmtime(out)
-    return any(os.path.getmtime(s) > t for s in (SRC, SRC_MATCH, HDR, __file__))
+    return any(os.path.getmtime(s) > t for s in (SRC, SRC_MATCH, SRC_WINDOW, HDR, __file__))
 
 
 def build(force: bool = False, verbose: bool = False) -> dict:
@@ -42,7 +43,7 @@ def build(force: bool = False, verbose: bool = False) -> dict:
         paths[name] = out
         if force or _stale(out):
             cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
-                   "-Wall", "-Wno-unknown-pragmas", *extra, "-o", out + ".tmp", SRC, SRC_MATCH]
+                   "-Wall", "-Wno-unknown-pragmas", *extra, "-o", out + ".tmp", SRC, SRC_MATCH, SRC_WINDOW]
             if verbose:
                 print(" ".join(cmd), file=sys.stderr)
             procs.append((out, subprocess.Popen(cmd)))

@@ -124,6 +124,52 @@ int orc_linearize_edges(const orc_problem* p, double* err, double* J_point, doub
 int orc_normal_equations(const orc_problem* p, double lambda, double* H, double* b, double* x_schur,
                          int cap);
 
+/* Flat map tables read by Map::AddKeyFrame's local-BA set-up
+ * (src/Map.cpp:140-145): keyframes with their LEFT (0) / WIDE (1)
+ * observations, map points with the keyframes bound to them
+ * (MapPoint::GetAllKeyFrame), the essential graph, the rig. */
+typedef struct orc_map_tables {
+  int32_t n_keyframes;
+  const int64_t* kf_id;       /* [K] Frame::id */
+  const int32_t* obs_begin;   /* [K + 1] */
+  const int32_t* obs_point;   /* [O] map point index */
+  const uint8_t* obs_object;  /* [O] 0 LEFT, 1 WIDE */
+  const float* obs_uv;        /* [O][2] */
+  const float* obs_ur;        /* [O] u_right, -1 when none */
+  const uint8_t* obs_octave;  /* [O] */
+  int32_t n_points;
+  const int32_t* mp_kf_begin; /* [P + 1] */
+  const int32_t* mp_kf;       /* keyframe indices */
+  const int32_t* ess_begin;   /* [K + 1] */
+  const int32_t* ess_adj;
+  const float* inv_sigma2_left;  /* per octave */
+  const float* inv_sigma2_wide;
+} orc_map_tables;
+
+/* The local-BA window and its problem in BAoptimizer insertion order. */
+typedef struct orc_window_out {
+  uint8_t* kf_role;      /* [K] bit 0 optimised, bit 1 anchor (fixed); may be NULL */
+  int32_t* pose_kf;      /* [<= K] map keyframe of each problem pose */
+  uint8_t* pose_fixed;   /* [<= K] */
+  int32_t* point_mp;     /* [<= P] map point of each problem point */
+  uint8_t* point_fixed;  /* [<= P] ThisMapPointBeFix */
+  int32_t max_edges;
+  uint8_t* edge_type;
+  int32_t* edge_pose;
+  int32_t* edge_point;
+  int32_t* edge_cam;     /* 0 LEFT, 1 WIDE */
+  float* edge_obs;       /* [E][3] u v u_right (0 for mono edges) */
+  float* edge_info;
+  float* edge_delta;
+  int32_t n_local, n_anchor, n_poses, n_points, n_edges;
+} orc_window_out;
+
+/* GrabLocalMap_Mappoint(cur, hop), GrabAnchorKeyFrames, the new keyframe
+ * added, then BoundleAdjustment's vertex/edge insertion with
+ * ThisMapPointBeFix (window_oracle.cpp).  Returns 0, -1 on bad arguments,
+ * -2 when more than max_edges edges. */
+int orc_local_window(const orc_map_tables* m, int32_t cur, int32_t hop, orc_window_out* out);
+
 /* Building blocks for known-answer tests. */
 void orc_se3_exp(const double update[6], double qt_out[7]);
 void orc_mat44f_to_qt(const float T[16], double qt_out[7]);

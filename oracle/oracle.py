@@ -317,3 +317,84 @@ def stereo_match(sb, n_threads: int = 1):
                        _ptr(k["rb"], c_i), _ptr(k["rxy"], c_f), _ptr(k["ro"], c_i), _ptr(k["rd"], c_u8),
                        _ptr(u, c_f), _ptr(d, c_f))
     return u, d
+
+
+class OrcMap(ctypes.Structure):
+    _fields_ = [
+        ("n_keyframes", ctypes.c_int32), ("kf_id", ctypes.POINTER(ctypes.c_int64)), ("obs_begin", c_i32_p),
+        ("obs_point", c_i32_p), ("obs_object", c_u8_p), ("obs_uv", c_float_p), ("obs_ur", c_float_p),
+        ("obs_octave", c_u8_p), ("n_points", ctypes.c_int32), ("mp_kf_begin", c_i32_p), ("mp_kf", c_i32_p),
+        ("ess_begin", c_i32_p), ("ess_adj", c_i32_p), ("inv_sigma2_left", c_float_p),
+        ("inv_sigma2_wide", c_float_p),
+    ]
+
+
+class OrcWindowOut(ctypes.Structure):
+    _fields_ = [
+        ("kf_role", c_u8_p), ("pose_kf", c_i32_p), ("pose_fixed", c_u8_p), ("point_mp", c_i32_p),
+        ("point_fixed", c_u8_p), ("max_edges", ctypes.c_int32), ("edge_type", c_u8_p), ("edge_pose", c_i32_p),
+        ("edge_point", c_i32_p), ("edge_cam", c_i32_p), ("edge_obs", c_float_p), ("edge_info", c_float_p),
+        ("edge_delta", c_float_p), ("n_local", ctypes.c_int32), ("n_anchor", ctypes.c_int32),
+        ("n_poses", ctypes.c_int32), ("n_points", ctypes.c_int32), ("n_edges", ctypes.c_int32),
+    ]
+
+
+def local_window(m, cur: int, hop: int = 1) -> dict:
+    """Map::AddKeyFrame's local-BA set-up on a synth.MapTables: the window
+    (kf_role bit 0 optimised, bit 1 anchor), the problem's vertices in
+    BAoptimizer insertion order and its edges (window_oracle.cpp)."""
+    L = lib(False)
+    if not hasattr(L, "_win_sig"):
+        L.orc_local_window.argtypes = [ctypes.POINTER(OrcMap), ctypes.c_int32, ctypes.c_int32,
+                                       ctypes.POINTER(OrcWindowOut)]
+        L._win_sig = True
+    a = lambda x, dt: np.ascontiguousarray(x, dt)  # noqa: E731
+    k = dict(id=a(m.kf_id, np.int64), ob=a(m.obs_begin, np.int32), op=a(m.obs_point, np.int32),
+             oo=a(m.obs_object, np.uint8), uv=a(m.obs_uv, np.float32), ur=a(m.obs_ur, np.float32),
+             oc=a(m.obs_octave, np.uint8), mb=a(m.mp_kf_begin, np.int32), mk=a(m.mp_kf, np.int32),
+             eb=a(m.ess_begin, np.int32), ea=a(m.ess_adj, np.int32), sl=a(m.inv_sigma2_left, np.float32),
+             sw=a(m.inv_sigma2_wide, np.float32))
+    s = OrcMap(m.n_keyframes, k["id"].ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), _ptr(k["ob"], c_i32_p),
+               _ptr(k["op"], c_i32_p), _ptr(k["oo"], c_u8_p), _ptr(k["uv"], c_float_p), _ptr(k["ur"], c_float_p),
+               _ptr(k["oc"], c_u8_p), m.n_points, _ptr(k["mb"], c_i32_p), _ptr(k["mk"], c_i32_p),
+               _ptr(k["eb"], c_i32_p), _ptr(k["ea"], c_i32_p), _ptr(k["sl"], c_float_p), _ptr(k["sw"], c_float_p))
+    nk, cap = m.n_keyframes, 2 * len(m.obs_point) + 1  # a keyframe can be anchor and member
+    o = dict(kf_role=np.zeros(nk, np.uint8), pose_kf=np.zeros(nk, np.int32), pose_fixed=np.zeros(nk, np.uint8),
+             point_mp=np.zeros(m.n_points, np.int32), point_fixed=np.zeros(m.n_points, np.uint8),
+             edge_type=np.zeros(cap, np.uint8), edge_pose=np.zeros(cap, np.int32), edge_point=np.zeros(cap, np.int32),
+             edge_cam=np.zeros(cap, np.int32), edge_obs=np.zeros((cap, 3), np.float32),
+             edge_info=np.zeros(cap, np.float32), edge_delta=np.zeros(cap, np.float32))
+    w = OrcWindowOut(_ptr(o["kf_role"], c_u8_p), _ptr(o["pose_kf"], c_i32_p), _ptr(o["pose_fixed"], c_u8_p),
+                     _ptr(o["point_mp"], c_i32_p), _ptr(o["point_fixed"], c_u8_p), cap,
+                     _ptr(o["edge_type"], c_u8_p), _ptr(o["edge_pose"], c_i32_p), _ptr(o["edge_point"], c_i32_p),
+                     _ptr(o["edge_cam"], c_i32_p), _ptr(o["edge_obs"], c_float_p), _ptr(o["edge_info"], c_float_p),
+                     _ptr(o["edge_delta"], c_float_p), 0, 0, 0, 0, 0)
+    rc = L.orc_local_window(ctypes.byref(s), cur, hop, ctypes.byref(w))
+    if rc != 0:
+        raise RuntimeError(f"orc_local_window returned {rc}")
+    npo, npt, ne = w.n_poses, w.n_points, w.n_edges
+    for key in ("pose_kf", "pose_fixed"):
+        o[key] = o[key][:npo]
+    for key in ("point_mp", "point_fixed"):
+        o[key] = o[key][:npt]
+    for key in ("edge_type", "edge_pose", "edge_point", "edge_cam", "edge_obs", "edge_info", "edge_delta"):
+        o[key] = o[key][:ne]
+    o.update(n_local=w.n_local, n_anchor=w.n_anchor)
+    return o
+
+
+def window_problem(m, w: dict):
+    """The assembled window as a synth.Problem (camera 0 LEFT with
+    T_cam_body = I and the stereo bf, camera 1 WIDE), for the oracle solver."""
+    from mcvslam_gb300 import synth
+
+    E = len(w["edge_type"])
+    return synth.Problem(
+        cam_K=np.stack([m.K_left, m.K_wide]).astype(np.float32), cam_bf=np.array([m.bf, 0.0], np.float32),
+        cam_Tcb=np.stack([np.eye(4, dtype=np.float32).reshape(16), m.T_wide_body]).astype(np.float32),
+        cam_size=np.array([[512, 512], [512, 512]], np.int32),
+        pose_Tcw=m.kf_Tcw[w["pose_kf"]].astype(np.float32), pose_fixed=w["pose_fixed"].astype(np.uint8),
+        point_Xw=m.mp_Xw[w["point_mp"]].astype(np.float32), point_fixed=w["point_fixed"].astype(np.uint8),
+        edge_type=w["edge_type"], edge_pose=w["edge_pose"], edge_point=w["edge_point"], edge_cam=w["edge_cam"],
+        edge_obs=w["edge_obs"], edge_info=w["edge_info"], edge_delta=w["edge_delta"],
+        edge_robust=np.ones(E, np.uint8), edge_level=np.zeros(E, np.uint8), name="local_window")
