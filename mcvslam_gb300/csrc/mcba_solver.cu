@@ -37,6 +37,7 @@
 #include <vector>
 
 #include "mcba_chol.h"
+#include "mcba_chol_tiled.h"
 #include "mcba_device.cuh"
 #include "mcba_internal.h"
 
@@ -697,130 +698,6 @@ __global__ void __launch_bounds__(64 * kAsmGroups) k_schur_assemble(Bufs B, int 
   }
 }
 
-// ------------------------------------------------ blocked Cholesky --
-// Diagonal tile k: LL^T in shared memory; a pivot <= 0 marks the solve as
-// failed (SimplicialLLT's info() != Success, linear_solver_eigen.h:118-126).
-// The reciprocals of the diagonal go to dinv for the triangular solves.
-__global__ void __launch_bounds__(256) k_chol_potrf(double* S, double* dinv, int ld, int k, LMState* lm) {
-  __shared__ double T[kNB][kNB + 1];
-  __shared__ double rinv;
-  const int o = k * kNB;
-  for (int idx = threadIdx.x; idx < kNB * kNB; idx += blockDim.x) {
-    const int i = idx / kNB, j = idx % kNB;
-    T[i][j] = (j <= i) ? S[(size_t)(o + i) * ld + o + j] : 0.0;
-  }
-  __syncthreads();
-  for (int kk = 0; kk < kNB; ++kk) {
-    if (threadIdx.x == 0) {
-      const double d = T[kk][kk];
-      if (d <= 0.0) lm->solve_ok = 0;
-      const double r = sqrt(d);
-      T[kk][kk] = r;
-      rinv = 1.0 / r;
-      dinv[o + kk] = rinv;
-    }
-    __syncthreads();
-    if (threadIdx.x > kk && threadIdx.x < kNB) T[threadIdx.x][kk] *= rinv;
-    __syncthreads();
-    for (int idx = threadIdx.x; idx < kNB * kNB; idx += blockDim.x) {
-      const int i = idx / kNB, j = idx % kNB;
-      if (j > kk && i >= j) T[i][j] -= T[i][kk] * T[j][kk];
-    }
-    __syncthreads();
-  }
-  for (int idx = threadIdx.x; idx < kNB * kNB; idx += blockDim.x) {
-    const int i = idx / kNB, j = idx % kNB;
-    if (j <= i) S[(size_t)(o + i) * ld + o + j] = T[i][j];
-  }
-}
-
-// Rows below the diagonal tile (8 rows per CTA, the extra b row included):
-// L_ik = A_ik L_kk^-T.
-__global__ void __launch_bounds__(256) k_chol_trsm(double* S, const double* dinv, int ld, int k, int nrows) {
-  __shared__ double L[kNB][kNB + 1];
-  __shared__ double X[8][kNB + 1];
-  __shared__ double di[kNB];
-  const int o = k * kNB;
-  const int row0 = o + kNB + blockIdx.x * 8;
-  for (int idx = threadIdx.x; idx < kNB * kNB; idx += blockDim.x) {
-    const int i = idx / kNB, j = idx % kNB;
-    L[i][j] = (j <= i) ? S[(size_t)(o + i) * ld + o + j] : 0.0;
-  }
-  if (threadIdx.x < kNB) di[threadIdx.x] = dinv[o + threadIdx.x];
-  const int r = threadIdx.x / kNB, c = threadIdx.x % kNB;
-  const int grow = row0 + r;
-  X[r][c] = (grow < nrows) ? S[(size_t)grow * ld + o + c] : 0.0;
-  __syncthreads();
-  for (int kk = 0; kk < kNB; ++kk) {
-    if (c == kk) X[r][kk] *= di[kk];
-    __syncthreads();
-    if (c > kk) X[r][c] -= X[r][kk] * L[c][kk];
-    __syncthreads();
-  }
-  if (grow < nrows) S[(size_t)grow * ld + o + c] = X[r][c];
-}
-
-// Trailing update A_ij -= L_ik L_jk^T on 8x8 sub-tiles of the lower part.
-__global__ void __launch_bounds__(64) k_chol_syrk(double* S, int ld, int k, int nrows) {
-  const int o = k * kNB;
-  const int base = o + kNB;
-  const int sc = blockIdx.x, sr = blockIdx.y;  // sub-tile column / row (8-wide) from base
-  const int col0 = base + sc * 8, row0 = base + sr * 8;
-  if (col0 > row0 + 7 || col0 >= ld) return;
-  __shared__ double Li[8][kNB + 1], Lj[8][kNB + 1];
-  for (int idx = threadIdx.x; idx < 8 * kNB; idx += blockDim.x) {
-    const int rr = idx / kNB, cc = idx % kNB;
-    Li[rr][cc] = (row0 + rr < nrows) ? S[(size_t)(row0 + rr) * ld + o + cc] : 0.0;
-    Lj[rr][cc] = S[(size_t)(col0 + rr) * ld + o + cc];
-  }
-  __syncthreads();
-  const int rr = threadIdx.x / 8, cc = threadIdx.x % 8;
-  const int grow = row0 + rr, gcol = col0 + cc;
-  if (grow >= nrows || gcol > grow) return;
-  double s = 0.0;
-#pragma unroll 8
-  for (int q = 0; q < kNB; ++q) s += Li[rr][q] * Lj[cc][q];
-  S[(size_t)grow * ld + gcol] -= s;
-}
-
-// L^T x = y with y in the extra row; writes x_p when the factorisation
-// succeeded.  Each tile column is first staged in shared memory.
-__global__ void __launch_bounds__(256) k_chol_backsolve(const double* S, const double* dinv, int ld, int n,
-                                                        double* x, LMState* lm) {
-  if (!lm->solve_ok) return;
-  __shared__ double xs[4096 + kNB];
-  __shared__ double part[8][kNB];
-  __shared__ double Lt[kNB][kNB + 1];
-  const double* y = S + (size_t)ld * ld;
-  const int nt = ld / kNB;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int I = nt - 1; I >= 0; --I) {
-    const int o = I * kNB;
-    double acc = 0.0;
-#pragma unroll 4
-    for (int kr = o + kNB + wid; kr < ld; kr += 8) acc += S[(size_t)kr * ld + o + lane] * xs[kr];
-    part[wid][lane] = acc;
-    for (int idx = threadIdx.x; idx < kNB * kNB; idx += blockDim.x) {
-      const int i = idx / kNB, j = idx % kNB;
-      Lt[i][j] = (j <= i) ? S[(size_t)(o + i) * ld + o + j] : 0.0;
-    }
-    __syncthreads();
-    if (wid == 0) {
-      double rc = y[o + lane];
-#pragma unroll
-      for (int w = 0; w < 8; ++w) rc -= part[w][lane];
-      const double dl = dinv[o + lane];
-      for (int c = kNB - 1; c >= 0; --c) {
-        const double xc = __shfl_sync(0xffffffffu, rc * dl, c);
-        if (lane < c) rc -= Lt[c][lane] * xc;
-        if (lane == c) xs[o + c] = xc;
-      }
-    }
-    __syncthreads();
-  }
-  for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = xs[i];
-}
-
 // Landmark back-substitution (block_solver.hpp:420-446) and point update,
 // plus the point part of computeScale (optimization_algorithm_levenberg.cpp:159-165).
 // Four lanes per point: lane s of the group walks edges s, s+4, .. of the
@@ -1174,6 +1051,7 @@ class Solver {
   size_t evnext = 0;
   Launch L{};
   CholPlan chol;
+  TiledChol tchol;  // side stream and events of the tiled solve (systems beyond the cluster solve)
   int chol_ld = -1, chol_n = -1;
   bool uploaded = false;
   int64_t launches = 0;
@@ -1209,6 +1087,7 @@ class Solver {
     cudaSetDevice(device);
     if (stream) cudaStreamSynchronize(stream);
     graph_release();
+    chol_tiled_release(&tchol);
     DBuf<double>* ds[] = {&pose_qt[0], &pose_qt[1], &Xd[0], &Xd[1], &pose_qt0, &Xd0,
                           &Hpp, &bp, &S, &cws, &dinv, &x, &cost_part, &scale_part, &chi2_out};
     for (auto* d : ds) d->release();
@@ -1574,23 +1453,9 @@ void launch_trial(Solver* s, const Bufs& B, const Launch& L, PhaseClock& pc, cud
         s->launches++;
         return;
       }
-      for (int k = 0; k < L.tiles; ++k) {
-        k_chol_potrf<<<1, 256, 0, st>>>(B.S, B.dinv, L.ld, k, B.lm);
-        s->launches++;
-        const int below = L.nrows - (k + 1) * kNB;
-        if (below > 0) {
-          k_chol_trsm<<<(below + 7) / 8, 256, 0, st>>>(B.S, B.dinv, L.ld, k, L.nrows);
-          s->launches++;
-          const int rem_cols = L.ld - (k + 1) * kNB;
-          if (rem_cols > 0) {
-            dim3 g(rem_cols / 8, (below + 7) / 8);
-            k_chol_syrk<<<g, 64, 0, st>>>(B.S, L.ld, k, L.nrows);
-            s->launches++;
-          }
-        }
-      }
-      k_chol_backsolve<<<1, 256, 0, st>>>(B.S, B.dinv, L.ld, L.n, B.x, B.lm);
-      s->launches++;
+      long long nl = 0;
+      chol_tiled_launch(s->tchol, B.S, B.cws, L.ld, L.n, B.x, &B.lm->solve_ok, st, &nl);
+      s->launches += nl;
       // the tiled factorisation works in place and fills absent blocks in;
       // the next trial's assembly writes only the present blocks, so S
       // returns to zeros (identity padding) here
@@ -1627,7 +1492,7 @@ int alloc_numerics(Solver* s, std::string* err) {
   CK(s->ppart.ensure(std::max<size_t>(1, (size_t)L.npc * 36 * ab)));
   CK(s->qpart.ensure(std::max<size_t>(1, (size_t)L.nchunk * 6 * ab)));
   CK(s->S.ensure((size_t)(L.ld + kNB) * L.ld));
-  CK(s->cws.ensure((size_t)(L.ld + kNB) * L.ld));
+  CK(s->cws.ensure(std::max((size_t)(L.ld + kNB) * L.ld, chol_tiled_ws_doubles(L.ld))));
   CK(s->dinv.ensure(L.ld));
   CK(s->x.ensure(std::max(nx, 1)));
   CK(s->cost_part.ensure(L.ncost));
@@ -1966,7 +1831,8 @@ int solver_upload(Solver* s, const HostProblem& hp, const Structure* hst, Struct
   L.n = n;
   L.npc = z.npc;
   L.nblk = z.nblk;
-  L.ld = std::max(kNB, ((n + kNB - 1) / kNB) * kNB);
+  // systems beyond the cluster solve (384 unknowns) take the tiled solve
+  L.ld = n > 384 ? chol_tiled_stride(n) : std::max(kNB, ((n + kNB - 1) / kNB) * kNB);
   L.tiles = L.ld / kNB;
   L.nrows = L.ld + 1;  // the b_schur row
   L.ncost = (z.E + 255) / 256;
@@ -1983,6 +1849,12 @@ int solver_upload(Solver* s, const HostProblem& hp, const Structure* hst, Struct
     if (L.ld <= kClusterCholMaxLd && L.n > 0) chol_cluster_plan(L.ld, L.n, &s->chol);
     s->chol_ld = L.ld;
     s->chol_n = L.n;
+  }
+  if (!s->chol.ok && L.n > 0) {
+    if (chol_tiled_setup(&s->tchol) != cudaSuccess) {
+      if (err) *err = "tiled Cholesky set-up failed";
+      return MCBA_ERR_CUDA;
+    }
   }
   out.h2d += bytes;
   s->uploaded = true;
