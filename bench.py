@@ -164,6 +164,19 @@ def read_peaks():
         return 6800.0, "fallback"
 
 
+def fp64_peak(local: int):
+    """(GFLOP/s, source) of FP64 FMA: measured on the device by the library's
+    saturating FMA kernel, else the part's nominal rate."""
+    import ctypes
+
+    from mcvslam_gb300 import _native
+
+    g = ctypes.c_double(0.0)
+    if _native.lib().mcba_fp64_fma_rate(local, ctypes.byref(g)) == 0 and g.value > 0:
+        return g.value, "measured (mcba_fp64_fma_rate: saturating FMA kernel, CUDA events, best of 5)"
+    return FP64_NOMINAL_GFLOPS, "nominal FP64 rate of the part"
+
+
 def read_traffic(kernel: str):
     """Per-launch DRAM bytes of `kernel` recorded from an ncu capture in profiles/."""
     prof = os.path.join(ROOT, "profiles")
@@ -446,20 +459,24 @@ def run_mcba(args):
                 "algorithmic_bytes_per_launch": alg, "ms_per_launch": lin_ms,
                 "timing": "CUDA events around each launch, host-driven profiled pass of the same solves"}
     # the kernel with the largest share of the solve: the FP64 factorisation of
-    # the reduced camera system, bound by its pivot chain, not by a throughput
+    # the reduced camera system -- for up to 384 unknowns one cluster kernel
+    # bound by its pivot chain, beyond that the tiled kernels, bound by FP64
+    # throughput and their panel chain
     chol_ms = phase_ms[5] / max(phase_n[5], 1)
     nred = 6 * int(st0["n_free_poses"])
     flops = nred ** 3 / 3.0 + 4.0 * nred ** 2
-    fp64_peak = FP64_NOMINAL_GFLOPS
+    fp64_gf, fp64_src = fp64_peak(local)
+    achieved_gf = flops / (chol_ms / 1e3) / 1e9
     roofline_dominant = {
-        "kernel": "k_ldlt_cluster" if nred <= 384 else "k_chol_* (tiled)", "bound": "fp64 latency chain",
-        "achieved": flops / (chol_ms / 1e3) / 1e9,
-        "peak": fp64_peak, "unit": "GFLOP/s", "frac": flops / (chol_ms / 1e3) / 1e9 / fp64_peak,
-        "peak_source": "nominal FP64 rate of the part (no measured FP64 figure in MEASURED_PEAKS.json)",
-        "ms_per_launch": chol_ms, "n": nred,
+        "kernel": "k_ldlt_cluster" if nred <= 384 else "k_tchol_* (tiled)",
+        "bound": "fp64 latency chain" if nred <= 384 else "fp64 throughput + panel chain",
+        "achieved": achieved_gf, "peak": fp64_gf, "unit": "GFLOP/s", "frac": achieved_gf / fp64_gf,
+        "peak_source": fp64_src, "ms_per_launch": chol_ms, "n": nred,
+        "share_of_solve": float(phase_ms[5] / max(sum(prof_ms), 1e-9)),
+        "throughput_floor_ms": flops / (fp64_gf * 1e9) * 1e3,
         "chain_floor_us": nred * PIVOT_CHAIN_CYCLES / clk_mhz_nominal() if nred else None,
-        "note": "n^3/3 + 4 n^2 flops per solve; the floor is one dependent FP64 pivot step (about "
-                f"{PIVOT_CHAIN_CYCLES} cycles: FMA plus reciprocal with one Newton step) per unknown"}
+        "note": "n^3/3 + 4 n^2 flops per solve (factorisation and both substitutions); the chain floor is one "
+                f"dependent FP64 pivot step (about {PIVOT_CHAIN_CYCLES} cycles) per unknown"}
 
     # end-to-end leg through the C ABI with host buffers
     e2e = None
@@ -524,13 +541,20 @@ def run_config4(args):
     """Batched uneven problems: 64 local-BA windows (U(5,40) keyframes, U(50,300)
     points per keyframe) solved as branches of one CUDA graph, and 256
     pose-only frames (U(500,6000) observations, 10% outliers, 4 rounds x 10
-    iterations) in one persistent launch; mixed precision."""
+    iterations) in one persistent launch; mixed precision.
+
+    value = window edges linearised / s (device-resident graph launch); e2e =
+    the same through the C ABI with host buffers (64 loads, one batch
+    compile/upload, one graph launch, 64 read-backs); the per-window final-cost
+    gap of the mixed solves against FP64 solves of the same windows; the
+    roofline of k_linearize over the windows from host-driven profiled passes."""
     import torch
 
     from mcvslam_gb300 import ba, synth
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
+    iters = LBA_ITERS[2]
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
     wins = synth.window_batch(64)
     rng = np.random.default_rng(4100)
@@ -538,15 +562,16 @@ def run_config4(args):
     clocks = ClockSampler(local)
     with ba.LocalBABatch(wins, precision="mixed", device=local) as b:
         for _ in range(args.warmup):
-            b.solve(LBA_ITERS[2])
-        wms, edges = [], 0
+            b.solve(iters)
+        wms, edges, launches = [], 0, 0
         clocks.start()
         for _ in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()
-            stats, ms = b.solve(LBA_ITERS[2])
+            stats, ms = b.solve(iters)
             wms.append(ms)
             edges = sum(st["edges_linearized"] for st in stats)
+            launches += sum(st["kernel_launches"] for st in stats)
         for _ in range(args.warmup):
             ba.batch_pose_only(frames, "mixed", rounds=4, iterations=10, device=local)
         pms = []
@@ -555,7 +580,54 @@ def run_config4(args):
             torch.cuda.synchronize()
             pms.append(ba.batch_pose_only(frames, "mixed", rounds=4, iterations=10, device=local)["ms_device"])
         clk = clocks.stop()
+        mixed_states = b.states()
+        mixed_final = [st["final_chi2"] for st in stats]
     w_ms, p_ms = statistics.mean(wms), statistics.mean(pms)
+    # the same windows in FP64 plain, and the FP64 cost of each mixed result
+    with ba.LocalBABatch(wins, precision="fp64", device=local) as bf:
+        fstats, f_ms = bf.solve(iters)
+    gaps = []
+    for pr, (qt, X), fs in zip(wins, mixed_states, fstats):
+        chi_m = _fp64_cost(ba, pr, qt, X, local)
+        gaps.append((chi_m - fs["final_chi2"]) / fs["final_chi2"])
+    gaps = np.array(gaps)
+    # end to end through the C ABI with host buffers
+    e2e_ms, pe2e_ms = [], []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with ba.LocalBABatch(wins, precision="mixed", device=local) as b2:
+            b2.solve(iters)
+            b2.states()
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        ba.batch_pose_only(frames, "mixed", rounds=4, iterations=10, device=local)
+        if i >= args.warmup:
+            pe2e_ms.append(1e3 * (time.perf_counter() - t0))
+    h2d = int(sum(28 * w.n_edges + 28 * w.n_poses + 12 * w.n_points for w in wins))
+    d2h = int(sum(56 * w.n_poses + 24 * w.n_points for w in wins))
+    # k_linearize over every window: host-driven profiled passes
+    lin_ms, alg = 0.0, 0
+    for pr in wins:
+        sp = ba.Solver(precision="mixed", device=local, profile=True)
+        sp.load(pr)
+        sp.prepare()
+        sp.solve_prepared(iters)
+        stp = sp.solve_prepared(iters)
+        sp.close()
+        if stp["n_phase"][0]:
+            lin_ms += stp["ms_phase"][0] / stp["n_phase"][0]
+            alg += algorithmic_bytes_linearize(stp, "mixed")
+    peak, peak_kind = read_peaks()
+    lin_gbs = alg / (lin_ms / 1e3) / 1e9 if lin_ms > 0 else None
+    roofline = {"kernel": "k_linearize (64 windows, one launch each)", "bound": "hbm", "achieved": lin_gbs,
+                "peak": peak, "unit": "GB/s", "frac": lin_gbs / peak if lin_gbs else None, "peak_source": peak_kind,
+                "traffic": None, "algorithmic_bytes": alg, "ms_sum_of_launches": lin_ms,
+                "note": "sum of the 64 windows' algorithmic bytes over the sum of their event-timed launches; "
+                        "small windows are launch- and latency-bound"}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         from oracle import oracle
@@ -563,11 +635,17 @@ def run_config4(args):
         t0 = time.perf_counter()
         e_cpu = 0
         for pr in wins[:3]:
-            r = oracle.optimize(pr, LBA_ITERS[2], n_threads=1, log_cap=1)
+            r = oracle.optimize(pr, iters, n_threads=1, log_cap=1)
             e_cpu += r["n_active_edges"] * max(r["iterations_done"], 0)
         dt = time.perf_counter() - t0
+        t1 = time.perf_counter()
+        for fr in frames[:16]:
+            oracle.pose_optimization(fr, rounds=4, iters=10, chi2_thr=5.991)
+        dtp = time.perf_counter() - t1
         cpu = {"value": e_cpu / dt, "unit": "edges/s", "cores": 1, "kind": "port",
-               "sample": f"3 of the 64 windows, 10 LM iterations each, serial oracle, {dt:.1f} s"}
+               "sample": f"3 of the 64 windows, {iters} LM iterations each, serial oracle, {dt:.1f} s",
+               "pose_only_frames_per_s": 16 / dtp,
+               "pose_only_sample": f"16 of the 256 frames, 4 rounds x 10 iterations, serial oracle, {dtp:.1f} s"}
     if rank == 0:
         line = {
             "metric": "LM edges linearised/s, 64 local-BA windows in one graph launch", "value": edges / (w_ms / 1e3),
@@ -575,11 +653,20 @@ def run_config4(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic (seeded generator with the benchmark's shapes and noise model)",
             "config": {"workload": "config4_batched", "windows": len(wins),
-                       "window_edges": int(sum(w.n_edges for w in wins)), "lm_iterations": LBA_ITERS[2],
+                       "window_edges": int(sum(w.n_edges for w in wins)), "lm_iterations": iters,
                        "pose_only_frames": len(frames), "pose_only_edges": int(sum(f.n_edges for f in frames)),
                        "pose_only_ms": p_ms, "pose_only_frames_per_s": len(frames) / (p_ms / 1e3),
                        "l2": "flushed (256 MB write) before every step"},
-            "cpu_baseline": cpu, "clocks": clk,
+            "e2e": {"value": edges / (statistics.mean(e2e_ms) / 1e3), "unit": "edges/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": statistics.mean(e2e_ms),
+                    "pose_only_ms": statistics.mean(pe2e_ms),
+                    "pose_only_frames_per_s": len(frames) / (statistics.mean(pe2e_ms) / 1e3)},
+            "fp64_plain": {"ms_per_step": f_ms, "value": sum(s["edges_linearized"] for s in fstats) / (f_ms / 1e3)},
+            "precision_gap": {"per_window_final_cost_rel": [float(g) for g in gaps],
+                              "max_abs": float(np.abs(gaps).max()), "bound": 1e-6,
+                              "windows_within_bound": int((np.abs(gaps) <= 1e-6).sum()),
+                              "mixed_final_chi2": mixed_final},
+            "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
         }
         print(json.dumps(line), flush=True)
 

@@ -505,6 +505,13 @@ int mcba_reproj_backward(int32_t double_precision, int64_t n, const void* pose_q
                          const void* grad_res, void* g_pose, void* g_ext, void* g_X, void* J_pose,
                          void* J_ext, void* J_X, void* stream);
 
+/* ------------------------------------------------ device measurement -- */
+/* No counterpart in the reference: the FP64 FMA rate of `device` in
+ * GFLOP/s, measured with a saturating FMA kernel (CUDA events, best of five
+ * launches).  The roofline of the FP64 factorisation kernels is stated
+ * against it. */
+int mcba_fp64_fma_rate(int32_t device, double* gflops);
+
 /* ----------------------------------------- allocation-free robust cost -- */
 /* No counterpart in the reference: there every optimiser call allocates.
  * Sum of rho(e' Omega e) (the quantity of activeRobustChi2) over n mono edges

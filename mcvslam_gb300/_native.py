@@ -181,6 +181,7 @@ def _declare(L):
         "mcba_project_match_device": ([ctypes.POINTER(ProjectionBatchDesc), i32, i32, P, P, P, P], ctypes.c_int),
         "mcba_stereo_match": ([i32, ctypes.POINTER(StereoBatchDesc), P, P, c_double_p], ctypes.c_int),
         "mcba_stereo_match_device": ([ctypes.POINTER(StereoBatchDesc), i32, i32, P, P, P], ctypes.c_int),
+        "mcba_fp64_fma_rate": ([i32, c_double_p], ctypes.c_int),
         "mcba_robust_cost_noalloc": ([ctypes.c_int64, P, P, P, P, P, P, P, P, P, P], ctypes.c_int),
     }
     for name, (args, res) in sig.items():

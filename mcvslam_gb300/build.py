@@ -18,7 +18,7 @@ OUT = os.path.join(HERE, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 LIB = os.path.join(OUT, "libmcba.so")
 
-SOURCES = ["mcba_api.cpp", "mcba_solver.cu", "mcba_chol.cu", "mcba_chol_tiled.cu", "mcba_batch.cu", "mcba_reproj.cu", "mcba_noalloc.cu", "mcba_compile.cu", "mcba_match.cu", "mcba_project.cu", "mcba_stereo.cu", "mcba_window.cu"]
+SOURCES = ["mcba_api.cpp", "mcba_solver.cu", "mcba_chol.cu", "mcba_chol_tiled.cu", "mcba_batch.cu", "mcba_reproj.cu", "mcba_noalloc.cu", "mcba_compile.cu", "mcba_match.cu", "mcba_project.cu", "mcba_stereo.cu", "mcba_window.cu", "mcba_peak.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -439,7 +439,7 @@ namespace {
 // then loads into memory that is already mapped.
 std::mutex g_hp_mu;
 std::vector<HostProblem> g_hp_pool;
-constexpr size_t kHostPoolMax = 4;
+constexpr size_t kHostPoolMax = 64;  // as many as the solver workspaces kept per key
 }  // namespace
 
 int mcba_create(const mcba_options* opt, mcba_problem** out) {

@@ -1133,10 +1133,13 @@ class Solver {
 namespace {
 // Idle solvers (library-owned stream) kept for the next handle on the same
 // device and precision: device buffers, pinned staging, events, the stream
-// and the captured graph are reused instead of being allocated again.
+// and the captured graph are reused instead of being allocated again.  Up to
+// 64 per key, so a batch of windows created and destroyed on every call
+// (config 4: 64 local-BA windows) finds its workspaces again;
+// mcba_release_cached frees them.
 std::mutex g_pool_mu;
 std::vector<Solver*> g_pool;
-constexpr int kPoolPerKey = 2;
+constexpr int kPoolPerKey = 64;
 }  // namespace
 
 Solver* solver_create(int device, int precision, void* stream, std::string* err) {
