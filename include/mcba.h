@@ -458,6 +458,20 @@ int mcba_stereo_match_device(const mcba_stereo_batch* batch, int32_t n_left, int
 int mcba_batch_prepare(mcba_problem* const* problems, int32_t n);
 int mcba_batch_solve(mcba_problem* const* problems, int32_t n, int32_t iterations, mcba_stats* stats,
                      double* ms_device);
+/* The same windows (prepared by mcba_batch_prepare) in ONE persistent kernel
+ * launch: thread-block clusters stay resident and take windows from a device
+ * work queue, largest first, each cluster running one window's whole LM
+ * solve (BoundleAdjustment's optimize, include/PoseEstimation.hpp:102-105,
+ * with g2o's LM of optimization_algorithm_levenberg.cpp:56-143) with the
+ * same arithmetic in the same order as mcba_optimize, so every window's
+ * trial log, cost and estimates equal its single solve's.  The number of
+ * CTAs per window (the cluster size: 4, 8 or 16) is chosen on the first
+ * call for a batch by timing each candidate; *cluster_ctas (may be NULL)
+ * receives it.  All handles must share the device and the precision, and
+ * each window's reduced camera system must have at most 384 unknowns (64
+ * free keyframes); MCBA_ERR_INVALID otherwise. */
+int mcba_batch_solve_persistent(mcba_problem* const* problems, int32_t n, int32_t iterations, mcba_stats* stats,
+                                double* ms_device, int32_t* cluster_ctas);
 
 /* --------------------------------------------- batched pose-only solve -- */
 /* Many independent PoseEstimation::PoseOptimization problems

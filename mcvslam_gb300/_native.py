@@ -153,6 +153,8 @@ def _declare(L):
         "mcba_solve_prepared": ([P, i32, ctypes.POINTER(Stats)], ctypes.c_int),
         "mcba_batch_prepare": ([ctypes.POINTER(P), i32], ctypes.c_int),
         "mcba_batch_solve": ([ctypes.POINTER(P), i32, i32, ctypes.POINTER(Stats), c_double_p], ctypes.c_int),
+        "mcba_batch_solve_persistent": ([ctypes.POINTER(P), i32, i32, ctypes.POINTER(Stats), c_double_p,
+                                         ctypes.POINTER(i32)], ctypes.c_int),
         "mcba_fetch_state": ([P], ctypes.c_int),
         "mcba_trial_log_get": ([P, ctypes.POINTER(TrialLog), i32, c_i32_p], ctypes.c_int),
         "mcba_edge_chi2": ([P, c_double_p], ctypes.c_int),

@@ -282,7 +282,9 @@ def batch_pose_only(problems, precision: str = "mixed", rounds: int = 4, iterati
 
 
 class LocalBABatch:
-    """Many local-BA windows solved in one CUDA graph launch (mcba_batch_*)."""
+    """Many local-BA windows solved together (mcba_batch_*): as branches of one
+    CUDA graph, or (persistent=True) in one persistent launch whose clusters
+    take the windows from a device work queue."""
 
     def __init__(self, problems, precision: str = "mixed", device: int = 0):
         self.solvers = [Solver(precision=precision, device=device).load(pr) for pr in problems]
@@ -291,11 +293,17 @@ class LocalBABatch:
         self._arr = arr
         N.check(self.L.mcba_batch_prepare(arr, len(self.solvers)))
 
-    def solve(self, iterations: int = 10):
+    def solve(self, iterations: int = 10, persistent: bool = False):
         n = len(self.solvers)
         stats = (N.Stats * n)()
         ms = ctypes.c_double(0.0)
-        N.check(self.L.mcba_batch_solve(self._arr, n, iterations, stats, ctypes.byref(ms)), self.solvers[0].h)
+        if persistent:
+            ctas = ctypes.c_int32(0)
+            N.check(self.L.mcba_batch_solve_persistent(self._arr, n, iterations, stats, ctypes.byref(ms),
+                                                       ctypes.byref(ctas)), self.solvers[0].h)
+            self.cluster_ctas = ctas.value
+        else:
+            N.check(self.L.mcba_batch_solve(self._arr, n, iterations, stats, ctypes.byref(ms)), self.solvers[0].h)
         return [st.as_dict() for st in stats], ms.value
 
     def states(self):

@@ -892,6 +892,35 @@ int mcba_batch_solve(mcba_problem* const* problems, int32_t n, int32_t iteration
   return MCBA_OK;
 }
 
+int mcba_batch_solve_persistent(mcba_problem* const* problems, int32_t n, int32_t iterations, mcba_stats* stats,
+                                double* ms_device, int32_t* cluster_ctas) {
+  if (n < 0 || iterations < 0 || (n > 0 && !problems)) return MCBA_ERR_INVALID;
+  if (n == 0) return MCBA_OK;
+  std::vector<Solver*> ss(n);
+  for (int32_t i = 0; i < n; ++i) {
+    mcba_problem* p = problems[i];
+    if (!p) return MCBA_ERR_INVALID;
+    if (stats) std::memset(&stats[i], 0, sizeof(mcba_stats));
+    if (!p->prepared || !solver_has_upload(p->solver)) return fail(p, MCBA_ERR_INVALID, "mcba_batch_prepare first");
+    ss[i] = p->solver;
+  }
+  std::vector<SolveResult> res(n);
+  std::string e;
+  int ctas = 0;
+  const int r = solver_run_batch_persistent(ss.data(), n, run_options(problems[0], iterations), res.data(), ms_device,
+                                            &ctas, &e);
+  if (cluster_ctas) *cluster_ctas = ctas;
+  for (int32_t i = 0; i < n; ++i) {
+    mcba_problem* p = problems[i];
+    p->log = res[i].log;
+    p->hpp = res[i].hpp;
+    p->hpp_kf = p->st.Kf;
+    if (stats) fill_stats(&stats[i], res[i], &p->st, r);
+  }
+  if (r) return fail(problems[0], r, e);
+  return MCBA_OK;
+}
+
 int mcba_solve_prepared(mcba_problem* p, int32_t iterations, mcba_stats* st) {
   if (!p || iterations < 0) return fail(p, MCBA_ERR_INVALID, "bad argument");
   if (st) std::memset(st, 0, sizeof(*st));

@@ -207,6 +207,13 @@ int solver_run(Solver* s, const RunOptions& o, bool restore, SolveResult& out, s
 // once.  ms_device: event time of that launch.
 int solver_run_batch(Solver* const* ss, int n, const RunOptions& o, SolveResult* outs, double* ms_device,
                      std::string* err);
+// The same batch in one persistent launch: clusters of CTAs take the
+// windows from a device work queue and each runs a window's whole LM solve
+// (k_windows); the cluster size is chosen by timing the batch on its first
+// call.  Every problem must share the device and the precision, with at
+// most 384 reduced unknowns.  cluster_ctas (may be null): the chosen size.
+int solver_run_batch_persistent(Solver* const* ss, int n, const RunOptions& o, SolveResult* outs, double* ms_device,
+                                int* cluster_ctas, std::string* err);
 // Copies the current device state into hp.
 int solver_download(Solver* s, HostProblem& hp, SolveResult& out, std::string* err);
 bool solver_has_upload(const Solver* s);

@@ -24,6 +24,7 @@
 // The linearisation real type R is double (plain) or float (mixed); the
 // Cholesky, damping, gain ratio and retraction are FP64 in both.
 
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -37,6 +38,7 @@
 #include <vector>
 
 #include "mcba_chol.h"
+#include "mcba_chol_dev.cuh"
 #include "mcba_chol_tiled.h"
 #include "mcba_device.cuh"
 #include "mcba_internal.h"
@@ -259,10 +261,36 @@ __device__ __forceinline__ void store_row<double, 28>(double* p, const double* v
 }
 
 // ------------------------------------------------------------ kernels --
-__global__ void k_pose_lin(const double* __restrict__ qt, int n, PoseLinD* pd, PoseLinF* pf) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double* q = qt + 8 * (size_t)i;
+// The kernels' bodies run on a "block": the CTA of a plain launch, or a
+// group of warps of the persistent window kernel (k_windows), which runs
+// the same bodies for virtual block ids it is dealt.  id / tid / nthr
+// replace blockIdx.x / threadIdx.x / blockDim.x; sync() is __syncthreads for
+// a whole CTA and a named barrier of the block's warps otherwise.
+struct Blk {
+  int id, tid, nthr, bar;
+  __device__ __forceinline__ void sync() const {
+    if (bar == 0)
+      __syncthreads();
+    else
+      asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(nthr) : "memory");
+  }
+};
+__device__ __forceinline__ Blk grid_blk() { return Blk{(int)blockIdx.x, (int)threadIdx.x, (int)blockDim.x, 0}; }
+
+// block_sum over a Blk (same tree as dev::block_sum for the same block size)
+template <typename T>
+__device__ __forceinline__ T blk_sum(T x, T* sh, const Blk& b) {
+  const int lane = b.tid & 31, wid = b.tid >> 5, nw = b.nthr >> 5;
+  x = warp_sum(x);
+  b.sync();
+  if (lane == 0) sh[wid] = x;
+  b.sync();
+  T r = (lane < nw) ? sh[lane] : T(0);
+  r = warp_sum(r);
+  return r;
+}
+
+__device__ __forceinline__ void pose_lin_one(const double* q, PoseLinD* pd, PoseLinF* pf) {
   double Rm[9];
   quat_to_R(q, Rm);
   PoseLinD d;
@@ -277,8 +305,14 @@ __global__ void k_pose_lin(const double* __restrict__ qt, int n, PoseLinD* pd, P
 #pragma unroll
   for (int k = 0; k < 3; ++k)
     f.c[k] = (float)(-(Rm[k] * q[4] + Rm[3 + k] * q[5] + Rm[6 + k] * q[6]));
-  pd[i] = d;
-  pf[i] = f;
+  *pd = d;
+  *pf = f;
+}
+
+__global__ void k_pose_lin(const double* __restrict__ qt, int n, PoseLinD* pd, PoseLinF* pf) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  pose_lin_one(qt + 8 * (size_t)i, pd + i, pf + i);
 }
 
 __global__ void k_points_f(const double* __restrict__ X, int n, float4* Xf) {
@@ -289,11 +323,11 @@ __global__ void k_points_f(const double* __restrict__ X, int n, float4* Xf) {
 
 // Per-edge linearisation (buildSystem's edge loop, block_solver.hpp:490-506).
 template <typename R>
-__global__ void __launch_bounds__(kLinThreads) k_linearize(Bufs B) {
-  const int c = blockIdx.x;
+__device__ __forceinline__ void linearize_blk(const Bufs& B, const Blk& b, Acc<R> (*sh)[32]) {
+  const int c = b.id;
   const int jb = B.chunk_begin[c], je = B.chunk_begin[c + 1];
   const int ph = B.chunk_pose[c];
-  const int j = jb + threadIdx.x;
+  const int j = jb + b.tid;
   const StateView v = make_view(B, B.lm->cur);
   Acc<R> acc[32];
 #pragma unroll
@@ -366,17 +400,22 @@ __global__ void __launch_bounds__(kLinThreads) k_linearize(Bufs B) {
     }
   }
   if (ph >= 0) {
-    __shared__ Acc<R> sh[kLinThreads / 32][32];
     const Acc<R> mine = warp_reduce_scatter32_acc(acc);
-    sh[threadIdx.x >> 5][threadIdx.x & 31] = mine;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-      Acc<R> t = sh[0][threadIdx.x];
+    sh[b.tid >> 5][b.tid & 31] = mine;
+    b.sync();
+    if (b.tid < 32) {
+      Acc<R> t = sh[0][b.tid];
 #pragma unroll
-      for (int w = 1; w < kLinThreads / 32; ++w) t.add(sh[w][threadIdx.x]);
-      reinterpret_cast<Acc<R>*>(B.partials)[(size_t)c * 32 + threadIdx.x] = t;
+      for (int w = 1; w < kLinThreads / 32; ++w) t.add(sh[w][b.tid]);
+      reinterpret_cast<Acc<R>*>(B.partials)[(size_t)c * 32 + b.tid] = t;
     }
   }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kLinThreads) k_linearize(Bufs B) {
+  __shared__ Acc<R> sh[kLinThreads / 32][32];
+  linearize_blk<R>(B, grid_blk(), sh);
 }
 
 // a += p[c0 * stride] + .. + p[(c1 - 1) * stride], in that order; the loads
@@ -475,13 +514,13 @@ __device__ __forceinline__ unsigned long long abs_bits(double x) {
   return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
 }
 
+// Thread `t` of `nt` takes entries t, t + nt, ..; the maximum does not
+// depend on the split.
 template <typename R>
-__global__ void k_lambda_max(Bufs B, int Kf, int Lf) {
-  __shared__ unsigned long long sh[32];
-  if (B.lm->iteration != 0) return;
+__device__ __forceinline__ unsigned long long lambda_max_part(const Bufs& B, int Kf, int Lf, int t, int nt) {
   unsigned long long m = 0;
   const int n = 6 * Kf + 3 * Lf;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+  for (int k = t; k < n; k += nt) {
     unsigned long long v;
     if (k < 6 * Kf) {
       v = abs_bits(B.Hpp[(size_t)(k / 6) * 36 + 7 * (k % 6)]);
@@ -496,6 +535,15 @@ __global__ void k_lambda_max(Bufs B, int Kf, int Lf) {
     const unsigned long long v = __shfl_xor_sync(0xffffffffu, m, o);
     m = v > m ? v : m;
   }
+  return m;
+}
+
+template <typename R>
+__global__ void k_lambda_max(Bufs B, int Kf, int Lf) {
+  __shared__ unsigned long long sh[32];
+  if (B.lm->iteration != 0) return;
+  const unsigned long long m =
+      lambda_max_part<R>(B, Kf, Lf, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -505,11 +553,13 @@ __global__ void k_lambda_max(Bufs B, int Kf, int Lf) {
   }
 }
 
-__global__ void k_lambda_set(LMState* lm, double tau) {
+__device__ __forceinline__ void lambda_set(LMState* lm, double tau) {
   if (lm->iteration != 0) return;
   lm->lambda = tau * __longlong_as_double((long long)lm->lam_bits);
   lm->ni = 2.0;
 }
+
+__global__ void k_lambda_set(LMState* lm, double tau) { lambda_set(lm, tau); }
 
 template <typename R>
 __device__ __forceinline__ void damped_inverse(const R* Hu, R lam, R* Di) {
@@ -535,9 +585,7 @@ __device__ __forceinline__ void damped_inverse(const R* Hu, R lam, R* Di) {
 // from the FP64 point blocks, stored in the linearisation type:
 // pdv[l] = Dinv row-major (9) | Dinv b_l (3).
 template <typename R>
-__global__ void __launch_bounds__(128) k_point_dinv(Bufs B, int Lf) {
-  const int l = blockIdx.x * blockDim.x + threadIdx.x;
-  if (l >= Lf) return;
+__device__ __forceinline__ void point_dinv_one(const Bufs& B, int l) {
   double D[9];
   damped_inverse<double>(B.Hll + (size_t)l * 6, B.lm->lambda, D);
   const R* bl = Ptrs<R>::p(B.bl) + 3 * (size_t)l;
@@ -550,16 +598,22 @@ __global__ void __launch_bounds__(128) k_point_dinv(Bufs B, int Lf) {
   store_row<R, kPdv>(Ptrs<R>::p(B.pdv) + (size_t)l * kPdv, o);
 }
 
+template <typename R>
+__global__ void __launch_bounds__(128) k_point_dinv(Bufs B, int Lf) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l < Lf) point_dinv_one<R>(B, l);
+}
+
 // Y_e = Hpl_e Dinv for every edge with a free point and a free pose, walked in
 // the pose-sorted stream (one pose per CTA) so that q = sum_e Hpl_e Dinv b_l
 // -- the coefficient subtracted from b_p (block_solver.hpp:356-374) -- is
 // reduced per chunk without atomics.
 template <typename R>
-__global__ void __launch_bounds__(kLinThreads) k_schur_edge(Bufs B) {
-  const int c = blockIdx.x;
+__device__ __forceinline__ void schur_edge_blk(const Bufs& B, const Blk& b, Acc<R> (*sh)[kLinThreads / 32]) {
+  const int c = b.id;
   const int jb = B.chunk_begin[c], je = B.chunk_begin[c + 1];
   const int ph = B.chunk_pose[c];
-  const int j = jb + threadIdx.x;
+  const int j = jb + b.tid;
   Acc<R> qa[6];
 #pragma unroll
   for (int k = 0; k < 6; ++k) qa[k].zero();
@@ -586,31 +640,33 @@ __global__ void __launch_bounds__(kLinThreads) k_schur_edge(Bufs B) {
     }
   }
   if (ph >= 0) {
-    __shared__ Acc<R> sh[6][kLinThreads / 32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int lane = b.tid & 31, wid = b.tid >> 5;
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
       const Acc<R> w = warp_sum_acc(qa[k]);
       if (lane == 0) sh[k][wid] = w;
     }
-    __syncthreads();
-    if (threadIdx.x < 6) {
-      Acc<R> t = sh[threadIdx.x][0];
+    b.sync();
+    if (b.tid < 6) {
+      Acc<R> t = sh[b.tid][0];
 #pragma unroll
-      for (int w = 1; w < kLinThreads / 32; ++w) t.add(sh[threadIdx.x][w]);
-      reinterpret_cast<Acc<R>*>(B.qpart)[(size_t)c * 6 + threadIdx.x] = t;
+      for (int w = 1; w < kLinThreads / 32; ++w) t.add(sh[b.tid][w]);
+      reinterpret_cast<Acc<R>*>(B.qpart)[(size_t)c * 6 + b.tid] = t;
     }
   }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kLinThreads) k_schur_edge(Bufs B) {
+  __shared__ Acc<R> sh[6][kLinThreads / 32];
+  schur_edge_blk<R>(B, grid_blk(), sh);
 }
 
 // Reduced-camera block products over the pair list: one warp per chunk of
 // <= 128 pairs that all belong to one block; lanes accumulate whole 6x6
 // products in registers, then a reduce-scatter gives one partial per chunk.
 template <typename R>
-__global__ void __launch_bounds__(256) k_schur_pairs(Bufs B, int npc) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (warp >= npc) return;
+__device__ __forceinline__ void schur_pairs_warp(const Bufs& B, int warp, int lane) {
   const int p0 = B.pchunk_begin[warp], p1 = B.pchunk_begin[warp + 1];
   Acc<R> acc[32], acc2[4];
 #pragma unroll
@@ -648,6 +704,12 @@ __global__ void __launch_bounds__(256) k_schur_pairs(Bufs B, int npc) {
   }
 }
 
+template <typename R>
+__global__ void __launch_bounds__(256) k_schur_pairs(Bufs B, int npc) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp < npc) schur_pairs_warp<R>(B, warp, threadIdx.x & 31);
+}
+
 // S_ab = [a == b](Hpp_a + lambda I) - sum of the block's chunk partials, into
 // the dense FP64 reduced camera matrix (lower triangle is what the
 // factorisation reads).  Four groups of 64 threads each sum a quarter of the
@@ -657,10 +719,9 @@ __global__ void __launch_bounds__(256) k_schur_pairs(Bufs B, int npc) {
 constexpr int kAsmGroups = 4;
 
 template <typename R>
-__global__ void __launch_bounds__(64 * kAsmGroups) k_schur_assemble(Bufs B, int ld) {
-  __shared__ Acc<R> sh[kAsmGroups][36];
-  const int blk = blockIdx.x;
-  const int grp = threadIdx.x >> 6, t = threadIdx.x & 63;
+__device__ __forceinline__ void schur_assemble_blk(const Bufs& B, const Blk& b, int ld, Acc<R> (*sh)[36]) {
+  const int blk = b.id;
+  const int grp = b.tid >> 6, t = b.tid & 63;
   const int a = B.block_ab[2 * blk], bb = B.block_ab[2 * blk + 1];
   const int c0 = B.block_chunk_begin[blk], c1 = B.block_chunk_begin[blk + 1];
   if (t < 36) {
@@ -681,7 +742,7 @@ __global__ void __launch_bounds__(64 * kAsmGroups) k_schur_assemble(Bufs B, int 
     acc_range(qs, qp + t, B.pose_chunk_begin[a], B.pose_chunk_begin[a + 1], 6);
     B.S[(size_t)ld * ld + 6 * a + t] = B.bp[6 * (size_t)a + t] - qs.value();
   }
-  __syncthreads();
+  b.sync();
   if (grp != 0 || t >= 36) return;
   Acc<R> v = sh[0][t];
 #pragma unroll
@@ -698,6 +759,12 @@ __global__ void __launch_bounds__(64 * kAsmGroups) k_schur_assemble(Bufs B, int 
   }
 }
 
+template <typename R>
+__global__ void __launch_bounds__(64 * kAsmGroups) k_schur_assemble(Bufs B, int ld) {
+  __shared__ Acc<R> sh[kAsmGroups][36];
+  schur_assemble_blk<R>(B, grid_blk(), ld, sh);
+}
+
 // Landmark back-substitution (block_solver.hpp:420-446) and point update,
 // plus the point part of computeScale (optimization_algorithm_levenberg.cpp:159-165).
 // Four lanes per point: lane s of the group walks edges s, s+4, .. of the
@@ -708,9 +775,9 @@ constexpr int kPtLanes = 4;
 constexpr int kPtsPerBlock = 128 / kPtLanes;  // k_update runs 128-thread blocks
 
 template <typename R>
-__device__ __forceinline__ void backsub_block(const Bufs& B, int Lf, int n, int blk, double* sh) {
-  const int l = blk * kPtsPerBlock + (int)(threadIdx.x / kPtLanes);
-  const int sub = threadIdx.x % kPtLanes;
+__device__ __forceinline__ void backsub_block(const Bufs& B, int Lf, int n, int blk, double* sh, const Blk& b) {
+  const int l = blk * kPtsPerBlock + b.tid / kPtLanes;
+  const int sub = b.tid % kPtLanes;
   const int cur = B.lm->cur, cand = cur ^ 1;
   const double lam = B.lm->lambda;
   const bool ok = B.lm->solve_ok != 0;
@@ -759,15 +826,16 @@ __device__ __forceinline__ void backsub_block(const Bufs& B, int Lf, int n, int 
     reinterpret_cast<float*>(B.Xf[cand] + id)[q] = (float)nx;
     if (q == 0) reinterpret_cast<float*>(B.Xf[cand] + id)[3] = 0.f;
   }
-  const double tot = block_sum(sc, sh);
-  if (threadIdx.x == 0) B.scale_part[blk] = tot;
+  const double tot = blk_sum(sc, sh, b);
+  if (b.tid == 0) B.scale_part[blk] = tot;
 }
 
 // VertexSE3Expmap::oplusImpl on every free pose into the candidate buffer,
 // plus the pose part of computeScale.  Written to scale_part[slot].
 template <typename R>
-__device__ __forceinline__ void update_poses_block(const Bufs& B, int Kf, int slot0, int blk, double* sh) {
-  const int i = blk * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void update_poses_block(const Bufs& B, int Kf, int slot0, int blk, double* sh,
+                                                   const Blk& b) {
+  const int i = blk * b.nthr + b.tid;
   const int cur = B.lm->cur, cand = cur ^ 1;
   const double lam = B.lm->lambda;
   double sc = 0.0;
@@ -798,8 +866,8 @@ __device__ __forceinline__ void update_poses_block(const Bufs& B, int Kf, int sl
 #pragma unroll
     for (int k = 0; k < 6; ++k) sc += u[k] * (lam * u[k] + B.bp[6 * (size_t)i + k]);
   }
-  const double tot = block_sum(sc, sh);
-  if (threadIdx.x == 0) B.scale_part[slot0 + blk] = tot;
+  const double tot = blk_sum(sc, sh, b);
+  if (b.tid == 0) B.scale_part[slot0 + blk] = tot;
 }
 
 // One launch for both updates: the pose blocks (long FP64 exp chains) come
@@ -807,12 +875,18 @@ __device__ __forceinline__ void update_poses_block(const Bufs& B, int Kf, int sl
 // partials keep their slots (points first, then poses), so the sum order
 // does not depend on the launch layout.
 template <typename R>
+__device__ __forceinline__ void update_blk(const Bufs& B, const Blk& b, int Lf, int n, int Kf, int npose_blocks,
+                                           int npt_blocks, double* sh) {
+  if (b.id < npose_blocks)
+    update_poses_block<R>(B, Kf, npt_blocks, b.id, sh, b);
+  else
+    backsub_block<R>(B, Lf, n, b.id - npose_blocks, sh, b);
+}
+
+template <typename R>
 __global__ void k_update(Bufs B, int Lf, int n, int Kf, int npose_blocks, int npt_blocks) {
   __shared__ double sh[32];
-  if ((int)blockIdx.x < npose_blocks)
-    update_poses_block<R>(B, Kf, npt_blocks, blockIdx.x, sh);
-  else
-    backsub_block<R>(B, Lf, n, blockIdx.x - npose_blocks, sh);
+  update_blk<R>(B, grid_blk(), Lf, n, Kf, npose_blocks, npt_blocks, sh);
 }
 
 // activeRobustChi2 (sparse_optimizer.cpp:102-116) at the current (which = 0)
@@ -820,9 +894,8 @@ __global__ void k_update(Bufs B, int Lf, int n, int Kf, int npose_blocks, int np
 // summed per warp as float-float pairs (TwoSum, ~48-bit significand), so
 // the FP64 pipe, which is slow on this part, sees only the eight warp sums.
 template <typename R>
-__global__ void __launch_bounds__(256) k_cost(Bufs B, int E, int which) {
-  __shared__ double sh[32];
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void cost_blk(const Bufs& B, const Blk& b, int E, int which, double* sh) {
+  const int j = b.id * b.nthr + b.tid;
   const StateView v = make_view(B, B.lm->cur ^ which);
   R rho = R(0);
   if (j < E) {
@@ -837,29 +910,35 @@ __global__ void __launch_bounds__(256) k_cost(Bufs B, int E, int which) {
   a.zero();
   a.add(rho);
   a = warp_sum_acc(a);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int lane = b.tid & 31, wid = b.tid >> 5, nw = b.nthr >> 5;
   if (lane == 0) sh[wid] = a.value();
-  __syncthreads();
+  b.sync();
   if (wid == 0) {
     double t = (lane < nw) ? sh[lane] : 0.0;
     t = warp_sum(t);
-    if (lane == 0) B.cost_part[blockIdx.x] = t;
+    if (lane == 0) B.cost_part[b.id] = t;
   }
 }
 
-__device__ double sum_partials(const double* p, int n, double* sh) {
+template <typename R>
+__global__ void __launch_bounds__(256) k_cost(Bufs B, int E, int which) {
+  __shared__ double sh[32];
+  cost_blk<R>(B, grid_blk(), E, which, sh);
+}
+
+__device__ __forceinline__ void lm_begin_blk(const Bufs& B, const Blk& b, int ncost, double* sh) {
   double s = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) s += p[i];
-  return block_sum(s, sh);
+  for (int i = b.tid; i < ncost; i += b.nthr) s += B.cost_part[i];
+  const double c = blk_sum(s, sh, b);
+  if (b.tid == 0) {
+    B.lm->current_chi = c;
+    B.lm->initial_chi = c;
+  }
 }
 
 __global__ void k_lm_begin(Bufs B, int ncost) {
   __shared__ double sh[32];
-  const double c = sum_partials(B.cost_part, ncost, sh);
-  if (threadIdx.x == 0) {
-    B.lm->current_chi = c;
-    B.lm->initial_chi = c;
-  }
+  lm_begin_blk(B, grid_blk(), ncost, sh);
 }
 
 // One LM trial's decision (optimization_algorithm_levenberg.cpp:113-141).
@@ -867,14 +946,15 @@ __global__ void k_lm_begin(Bufs B, int ncost) {
 // sum_partials), and thread 0 works on a register copy of the LM state,
 // loaded before the sums and stored once at the end, so the decision is
 // not a chain of dependent global loads.
-__global__ void k_lm_decide(Bufs B, int ncost, int nscale, cudaGraphConditionalHandle h_trial, int in_graph) {
-  __shared__ double sh[64];
+// Returns, on the block's thread 0, whether another trial follows (0 or 1);
+// -1 on every other thread.
+__device__ __forceinline__ int lm_decide_blk(const Bufs& B, const Blk& b, int ncost, int nscale, double* sh) {
   LMState st;
-  if (threadIdx.x == 0) st = *B.lm;
+  if (b.tid == 0) st = *B.lm;
   double c = 0.0, d = 0.0;
-  for (int i = threadIdx.x; i < ncost; i += blockDim.x) c += B.cost_part[i];
-  for (int i = threadIdx.x; i < nscale; i += blockDim.x) d += B.scale_part[i];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int i = b.tid; i < ncost; i += b.nthr) c += B.cost_part[i];
+  for (int i = b.tid; i < nscale; i += b.nthr) d += B.scale_part[i];
+  const int lane = b.tid & 31, wid = b.tid >> 5, nw = b.nthr >> 5;
 #pragma unroll
   for (int o = 16; o >= 1; o >>= 1) {
     c += __shfl_xor_sync(0xffffffffu, c, o);
@@ -884,8 +964,8 @@ __global__ void k_lm_decide(Bufs B, int ncost, int nscale, cudaGraphConditionalH
     sh[wid] = c;
     sh[32 + wid] = d;
   }
-  __syncthreads();
-  if (wid != 0) return;
+  b.sync();
+  if (wid != 0) return -1;
   c = (lane < nw) ? sh[lane] : 0.0;
   d = (lane < nw) ? sh[32 + lane] : 0.0;
 #pragma unroll
@@ -893,7 +973,7 @@ __global__ void k_lm_decide(Bufs B, int ncost, int nscale, cudaGraphConditionalH
     c += __shfl_xor_sync(0xffffffffu, c, o);
     d += __shfl_xor_sync(0xffffffffu, d, o);
   }
-  if (lane != 0) return;
+  if (lane != 0) return -1;
   const double tempChi0 = c, scale0 = d;
   LMState* lm = &st;
   const double chi_before = lm->current_chi;
@@ -949,13 +1029,18 @@ __global__ void k_lm_decide(Bufs B, int ncost, int nscale, cudaGraphConditionalH
   // says otherwise
   lm->solve_ok = 1;
   *B.lm = st;
-  if (in_graph) cudaGraphSetConditional(h_trial, more ? 1u : 0u);
+  return more ? 1 : 0;
+}
+
+__global__ void k_lm_decide(Bufs B, int ncost, int nscale, cudaGraphConditionalHandle h_trial, int in_graph) {
+  __shared__ double sh[64];
+  const int more = lm_decide_blk(B, grid_blk(), ncost, nscale, sh);
+  if (more >= 0 && in_graph) cudaGraphSetConditional(h_trial, more ? 1u : 0u);
 }
 
 // LM state at the start of a solve (OptimizationAlgorithmLevenberg members
 // before iteration 0); in a graph it also arms the iteration loop.
-__global__ void k_lm_reset(LMState* lm, int max_trials, int max_log, int max_iters,
-                           cudaGraphConditionalHandle h_iter, int in_graph) {
+__device__ __forceinline__ void lm_reset(LMState* lm, int max_trials, int max_log, int max_iters) {
   LMState z{};
   z.cur = 0;
   z.solve_ok = 1;
@@ -965,6 +1050,11 @@ __global__ void k_lm_reset(LMState* lm, int max_trials, int max_log, int max_ite
   z.lambda = -1;
   z.ni = 2;
   *lm = z;
+}
+
+__global__ void k_lm_reset(LMState* lm, int max_trials, int max_log, int max_iters,
+                           cudaGraphConditionalHandle h_iter, int in_graph) {
+  lm_reset(lm, max_trials, max_log, max_iters);
   if (in_graph) cudaGraphSetConditional(h_iter, max_iters > 0 ? 1u : 0u);
 }
 
@@ -973,30 +1063,41 @@ __global__ void k_lm_reset(LMState* lm, int max_trials, int max_log, int max_ite
 // iteration count; the trial total is capped as a safety bound.
 // The loop body has run outer_runs times; that count alone bounds the loop,
 // whatever the trial loop did.
-__global__ void k_iter_end(LMState* lm, cudaGraphConditionalHandle h_iter) {
+__device__ __forceinline__ bool iter_end(LMState* lm) {
   lm->outer_runs++;
-  const bool go = !lm->terminate && lm->iteration < lm->max_iters && lm->outer_runs < lm->max_iters;
-  cudaGraphSetConditional(h_iter, go ? 1u : 0u);
+  return !lm->terminate && lm->iteration < lm->max_iters && lm->outer_runs < lm->max_iters;
+}
+
+__global__ void k_iter_end(LMState* lm, cudaGraphConditionalHandle h_iter) {
+  cudaGraphSetConditional(h_iter, iter_end(lm) ? 1u : 0u);
 }
 
 // Start of one LM iteration.  In the captured loop this also re-arms the
 // trial loop: a conditional handle's default value is applied only when the
 // whole graph is launched, so without this the inner WHILE would run zero
 // times from the second iteration on.
+__device__ __forceinline__ void iter_begin(LMState* lm) {
+  lm->trial = 0;
+  lm->trial_continue = 1;
+}
+
 __global__ void k_iter_begin(LMState* lm, cudaGraphConditionalHandle h_trial, int in_graph) {
   if (threadIdx.x == 0) {
-    lm->trial = 0;
-    lm->trial_continue = 1;
+    iter_begin(lm);
     if (in_graph) cudaGraphSetConditional(h_trial, 1u);
   }
 }
 
 // Zero the reduced camera matrix storage and put ones on the padding diagonal.
-__global__ void k_init_S(double* S, int ld, int n, size_t total) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+__device__ __forceinline__ void init_S_range(double* S, int ld, int n, size_t total, size_t i0, size_t step) {
+  for (size_t i = i0; i < total; i += step) {
     const size_t r = i / ld, c = i % ld;
     S[i] = (r == c && (int)r >= n && (int)r < ld) ? 1.0 : 0.0;
   }
+}
+
+__global__ void k_init_S(double* S, int ld, int n, size_t total) {
+  init_S_range(S, ld, n, total, blockIdx.x * (size_t)blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x);
 }
 
 __global__ void k_edge_chi2(const EdgeRec* recs, const float* obs, int E, StateView v, double* out) {
@@ -1008,6 +1109,177 @@ __global__ void k_edge_chi2(const EdgeRec* recs, const float* obs, int E, StateV
   transform(r, v, Pb, Pc);
   edge_error<double>(r, o, v, Pc, e, chi2);
   out[j] = chi2;
+}
+
+// ------------------------------------------------ persistent window kernel --
+// Many local-BA windows in one launch.  The grid is a set of thread-block
+// clusters of C CTAs that stay resident; each cluster takes the next window
+// from a device work queue (the host orders the windows by size, largest
+// first) and runs its whole LM solve: the phases of a single solve's
+// kernels, in the same order and over the same virtual blocks, with a
+// cluster barrier between phases, and the reduced camera system factored by
+// the cluster itself (the cluster LDL^T).  Sums therefore run in the same
+// order as in a single solve, and the results are the single solve's.
+//
+// A CTA has the factorisation's 320 threads.  Phases written for 256-thread
+// blocks run on warps 0-7 (named barrier 1); 128-thread blocks run two at a
+// time on warps 0-3 and 4-7 (barriers 1 and 2); per-thread and per-warp
+// work spreads over all ten warps of the cluster.
+namespace cg = cooperative_groups;
+constexpr int kWinThreads = chold::kThreads;
+
+struct WinDesc {
+  Bufs B;
+  const double* qt0;  // initial state restored at the start of the solve
+  const double* X0;
+  int nchunk, Kf, Lf, E, n, npc, nblk, ld, ncost, nscale_pts, nscale_pose, K, NP, max_log;
+  chold::Geo g;  // the factorisation's geometry for this launch's cluster size
+};
+
+struct WinArgs {
+  const WinDesc* w;
+  int nwin;
+  int* queue;  // next window (reset to 0 before each launch)
+  int iterations, max_trials;
+  double tau;
+};
+
+template <typename R>
+union WinShared {
+  Acc<R> lin[kLinThreads / 32][32];
+  Acc<R> se[6][kLinThreads / 32];
+  Acc<R> asmb[kAsmGroups][36];
+  double red[2][32];
+  double dec[64];
+};
+
+__device__ __forceinline__ void cluster_barrier() { cg::this_cluster().sync(); }
+
+// One window's LM solve by the calling cluster (the same control flow as
+// the captured graph of add_lm_subgraph, with restore).
+template <typename R>
+__device__ void window_solve(const WinArgs& a, const WinDesc& d, int rank, int C, WinShared<R>& sh, double* dsm) {
+  const Bufs& B = d.B;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int gt = rank * kWinThreads + tid, gn = C * kWinThreads;
+  const int gw = rank * (kWinThreads / 32) + warp, gwn = C * (kWinThreads / 32);
+  volatile LMState* vlm = B.lm;
+  // blocks of 256 threads on warps 0-7; blocks of 128 threads two at a time
+  auto run256 = [&](int nvb, auto&& body) {
+    if (tid >= 256) return;
+    for (int vb = rank; vb < nvb; vb += C) {
+      const Blk b{vb, tid, 256, 1};
+      body(b);
+      b.sync();  // the block's shared memory is free for the next one
+    }
+  };
+  auto run128 = [&](int nvb, auto&& body) {
+    if (tid >= 256) return;
+    const int half = tid >> 7;
+    for (int base = 2 * rank; base < nvb; base += 2 * C) {
+      const int vb = base + half;
+      if (vb >= nvb) break;
+      const Blk b{vb, tid & 127, 128, 1 + half};
+      body(b, sh.red[half]);
+      b.sync();
+    }
+  };
+
+  // ---- prologue: restore the initial state (both halves), S padding, x = 0,
+  //      LM state, initial cost
+  for (int i = gt; i < d.K; i += gn) {
+    double q[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) q[k] = d.qt0[8 * (size_t)i + k];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      B.pose_qt[0][8 * (size_t)i + k] = q[k];
+      B.pose_qt[1][8 * (size_t)i + k] = q[k];
+    }
+    pose_lin_one(q, B.pd[0] + i, B.pf[0] + i);
+    B.pd[1][i] = B.pd[0][i];
+    B.pf[1][i] = B.pf[0][i];
+  }
+  for (int i = gt; i < d.NP; i += gn) {
+    const double x0 = d.X0[3 * (size_t)i], x1 = d.X0[3 * (size_t)i + 1], x2 = d.X0[3 * (size_t)i + 2];
+    for (int b = 0; b < 2; ++b) {
+      B.Xd[b][3 * (size_t)i] = x0;
+      B.Xd[b][3 * (size_t)i + 1] = x1;
+      B.Xd[b][3 * (size_t)i + 2] = x2;
+      B.Xf[b][i] = make_float4((float)x0, (float)x1, (float)x2, 0.f);
+    }
+  }
+  init_S_range(B.S, d.ld, d.n, (size_t)(d.ld + kNB) * d.ld, gt, gn);
+  for (int i = gt; i < d.n + 3 * d.Lf; i += gn) B.x[i] = 0.0;
+  if (rank == 0 && tid == 0) lm_reset(B.lm, a.max_trials, d.max_log, a.iterations);
+  cluster_barrier();
+  run256(d.ncost, [&](const Blk& b) { cost_blk<R>(B, b, d.E, 0, sh.red[0]); });
+  cluster_barrier();
+  if (rank == 0 && tid < 256) lm_begin_blk(B, Blk{0, tid, 256, 1}, d.ncost, sh.red[0]);
+  cluster_barrier();
+
+  bool go = a.iterations > 0;
+  for (int it = 0; go && it < a.iterations; ++it) {
+    if (rank == 0 && tid == 0) iter_begin(B.lm);
+    run256(d.nchunk, [&](const Blk& b) { linearize_blk<R>(B, b, sh.lin); });
+    cluster_barrier();
+    for (int i = gw; i < d.Kf; i += gwn) pose_reduce_warp<R>(B, d.Kf, i, lane);
+    for (int l = gt; l < d.Lf; l += gn) point_reduce_thread<R>(B, d.Lf, l);
+    cluster_barrier();
+    if (vlm->iteration == 0) {
+      const unsigned long long m = lambda_max_part<R>(B, d.Kf, d.Lf, gt, gn);
+      if (lane == 0) atomicMax(&B.lm->lam_bits, m);
+      cluster_barrier();
+      if (rank == 0 && tid == 0) lambda_set(B.lm, a.tau);
+    }
+    cluster_barrier();
+    for (int t = 0; t < a.max_trials; ++t) {
+      if (d.Lf) {
+        for (int l = gt; l < d.Lf; l += gn) point_dinv_one<R>(B, l);
+        cluster_barrier();
+      }
+      if (d.Kf) {
+        run256(d.nchunk, [&](const Blk& b) { schur_edge_blk<R>(B, b, sh.se); });
+        cluster_barrier();
+        for (int i = gw; i < d.npc; i += gwn) schur_pairs_warp<R>(B, i, lane);
+        cluster_barrier();
+        run256(d.nblk, [&](const Blk& b) { schur_assemble_blk<R>(B, b, d.ld, sh.asmb); });
+        cluster_barrier();
+        chold::ldlt_cluster_run(B.S, B.cws, B.x, &B.lm->solve_ok, d.g, dsm);
+        chold::ldlt_cluster_retire(d.g, dsm, rank);
+      }
+      run128(d.nscale_pose + d.nscale_pts, [&](const Blk& b, double* shr) {
+        update_blk<R>(B, b, d.Lf, d.n, d.Kf, d.nscale_pose, d.nscale_pts, shr);
+      });
+      cluster_barrier();
+      run256(d.ncost, [&](const Blk& b) { cost_blk<R>(B, b, d.E, 1, sh.red[0]); });
+      cluster_barrier();
+      if (rank == 0 && tid < 256) lm_decide_blk(B, Blk{0, tid, 256, 1}, d.ncost, d.nscale_pts + d.nscale_pose, sh.dec);
+      cluster_barrier();
+      if (!vlm->trial_continue) break;
+    }
+    cluster_barrier();  // every thread has read trial_continue
+    if (rank == 0 && tid == 0) iter_end(B.lm);
+    cluster_barrier();
+    go = !vlm->terminate && vlm->iteration < vlm->max_iters && vlm->outer_runs < vlm->max_iters;
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kWinThreads, 1) k_windows(WinArgs a) {
+  extern __shared__ __align__(16) double dsm[];
+  __shared__ WinShared<R> sh;
+  __shared__ int s_win;
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank(), C = (int)cl.num_blocks();
+  for (int round = 0; round <= a.nwin; ++round) {
+    if (rank == 0 && threadIdx.x == 0) s_win = atomicAdd(a.queue, 1);
+    cl.sync();
+    const int w = *cl.map_shared_rank(&s_win, 0);
+    cl.sync();  // rank 0 overwrites s_win only after every CTA has read it
+    if (w >= a.nwin) break;
+    window_solve<R>(a, a.w[w], rank, C, sh, dsm);
+  }
 }
 
 }  // namespace
@@ -1975,6 +2247,277 @@ int solver_run_batch(Solver* const* ss, int n, const RunOptions& o, SolveResult*
     if (r) return r;
   }
   return MCBA_OK;
+}
+
+namespace {
+// The persistent window launch: descriptors and work queue on the device,
+// the cluster size the autotuner chose for the batch, and the captured
+// graph (queue reset + kernel), kept while the same workspaces, uploads and
+// options come back.
+struct PersistentBatch {
+  std::vector<long long> uids;
+  std::vector<int> gens;
+  std::vector<const void*> logs;
+  int iters = -1, trials = -1, device = -1, precision = -1;
+  double tau = 0.0;
+  int C = 0, nclusters = 0;
+  size_t smem = 0;
+  std::vector<std::pair<int, float>> tried;  // (CTAs per window, ms) of the autotuner
+  DBuf<WinDesc> desc;
+  DBuf<int> queue;
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t ge = nullptr;
+  void release_graph() {
+    if (ge) cudaGraphExecDestroy(ge);
+    if (g) cudaGraphDestroy(g);
+    ge = nullptr;
+    g = nullptr;
+  }
+};
+std::mutex g_pbatch_mu;
+PersistentBatch g_pbatch;
+
+// Descriptors of the windows (in launch order) for clusters of C CTAs, and
+// the dynamic shared memory the launch needs; false when a window's reduced
+// system does not fit the cluster factorisation.
+template <typename R>
+bool window_descs(Solver* const* ss, const std::vector<int>& order, const RunOptions& o, int C,
+                  std::vector<WinDesc>& out, size_t& smem, std::string* err) {
+  int dev = 0, max_smem = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaFuncAttributes fa{};
+  if (cudaFuncGetAttributes(&fa, k_windows<R>) != cudaSuccess) {
+    cudaGetLastError();
+    if (err) *err = "k_windows attributes";
+    return false;
+  }
+  const size_t reserve = fa.sharedSizeBytes + 1024;
+  out.clear();
+  smem = 0;
+  for (int i : order) {
+    Solver* s = ss[i];
+    const Launch& L = s->L;
+    WinDesc d{};
+    d.B = make_bufs(s);
+    d.qt0 = s->pose_qt0.p;
+    d.X0 = s->Xd0.p;
+    d.nchunk = L.nchunk;
+    d.Kf = L.Kf;
+    d.Lf = L.Lf;
+    d.E = L.E;
+    d.n = L.n;
+    d.npc = L.npc;
+    d.nblk = L.nblk;
+    d.ld = L.ld;
+    d.ncost = L.ncost;
+    d.nscale_pts = L.nscale_pts;
+    d.nscale_pose = L.nscale_pose;
+    d.K = L.K;
+    d.NP = L.NP;
+    d.max_log = std::max(1, o.iterations * o.max_trials);
+    const int nb = (L.n + chold::kB - 1) / chold::kB;
+    if (L.Kf && (nb > chold::kMaxBlk || chold::make_geo(16, L.ld, L.n, 1).ws_doubles() > (size_t)(L.ld + kNB) * L.ld)) {
+      if (err) *err = "a window's reduced camera system exceeds the persistent batch's limit (384 unknowns)";
+      return false;
+    }
+    int Rs = std::max(nb, 1);
+    while (Rs > std::min(nb, 3) && chold::make_geo(C, L.ld, L.n, Rs).total() * sizeof(double) + reserve > (size_t)max_smem)
+      --Rs;
+    d.g = chold::make_geo(C, L.ld, L.n, Rs);
+    const size_t bytes = L.Kf ? d.g.total() * sizeof(double) : 0;
+    if (bytes + reserve > (size_t)max_smem) {
+      if (err) *err = "a window's factorisation does not fit shared memory";
+      return false;
+    }
+    smem = std::max(smem, bytes);
+    out.push_back(d);
+  }
+  smem = std::max<size_t>(smem, 16);
+  return true;
+}
+
+template <typename R>
+cudaError_t launch_windows(const PersistentBatch& pb, int nwin, const RunOptions& o, int C, int nclusters, size_t smem,
+                           cudaStream_t st) {
+  WinArgs a{pb.desc.p, nwin, pb.queue.p, o.iterations, o.max_trials, o.tau};
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(C * nclusters, 1, 1);
+  cfg.blockDim = dim3(kWinThreads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr;
+  attr.id = cudaLaunchAttributeClusterDimension;
+  attr.val.clusterDim.x = C;
+  attr.val.clusterDim.y = 1;
+  attr.val.clusterDim.z = 1;
+  cfg.attrs = &attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_windows<R>, a);
+}
+
+// Clusters of C CTAs that can be resident at once with `smem` bytes each
+// (0 when the configuration cannot launch).
+template <typename R>
+int window_clusters(int C, size_t smem) {
+  int dev = 0, max_smem = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (cudaFuncSetAttribute(k_windows<R>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
+      cudaFuncSetAttribute(k_windows<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(C, 1, 1);
+  cfg.blockDim = dim3(kWinThreads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute attr;
+  attr.id = cudaLaunchAttributeClusterDimension;
+  attr.val.clusterDim.x = C;
+  attr.val.clusterDim.y = 1;
+  attr.val.clusterDim.z = 1;
+  cfg.attrs = &attr;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, k_windows<R>, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+template <typename R>
+int run_windows(Solver* const* ss, int n, const RunOptions& o, SolveResult* outs, double* ms_device, int* cluster_ctas,
+                std::string* err) {
+  Solver* s0 = ss[0];
+  cudaStream_t stm = s0->stream;
+  std::vector<long long> uids(n);
+  std::vector<int> gens(n);
+  std::vector<const void*> logs(n);
+  for (int i = 0; i < n; ++i) {
+    uids[i] = ss[i]->uid;
+    gens[i] = ss[i]->generation;
+    logs[i] = ss[i]->log.p;
+  }
+  PersistentBatch& pb = g_pbatch;
+  const bool same = pb.ge && pb.uids == uids && pb.gens == gens && pb.logs == logs && pb.iters == o.iterations &&
+                    pb.trials == o.max_trials && pb.tau == o.tau && pb.device == s0->device &&
+                    pb.precision == s0->precision;
+  if (!same) {
+    pb.release_graph();
+    // windows in descending size, so the largest start first
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+      const Launch &a = ss[x]->L, &b = ss[y]->L;
+      return (long long)a.E + 4LL * a.npc * 32 > (long long)b.E + 4LL * b.npc * 32;
+    });
+    CK(pb.queue.ensure(1));
+    CK(pb.desc.ensure(n));
+    // autotuner: CTAs per window (cluster size) by timing the whole batch,
+    // each candidate twice (the first run loads and warms up)
+    pb.tried.clear();
+    int bestC = 0, bestN = 0;
+    size_t bestSmem = 0;
+    float best = 0.f;
+    for (int C : {4, 8, 16}) {
+      std::vector<WinDesc> d;
+      size_t smem = 0;
+      if (!window_descs<R>(ss, order, o, C, d, smem, err)) return MCBA_ERR_INVALID;
+      const int ncl = window_clusters<R>(C, smem);
+      if (ncl < 1) continue;
+      const int nclusters = std::min(ncl, n);
+      CK(cudaMemcpyAsync(pb.desc.p, d.data(), d.size() * sizeof(WinDesc), cudaMemcpyHostToDevice, stm));
+      float ms = 0.f;
+      for (int rep = 0; rep < 2; ++rep) {
+        CK(cudaMemsetAsync(pb.queue.p, 0, sizeof(int), stm));
+        CK(cudaEventRecord(s0->ev[0], stm));
+        CK(launch_windows<R>(pb, n, o, C, nclusters, smem, stm));
+        CK(cudaEventRecord(s0->ev[1], stm));
+        CK(cudaStreamSynchronize(stm));
+        CK(cudaEventElapsedTime(&ms, s0->ev[0], s0->ev[1]));
+      }
+      pb.tried.emplace_back(C, ms);
+      if (!bestC || ms < best) {
+        best = ms;
+        bestC = C;
+        bestN = nclusters;
+        bestSmem = smem;
+      }
+    }
+    if (!bestC) {
+      if (err) *err = "no cluster size can launch the persistent window kernel";
+      return MCBA_ERR_CUDA;
+    }
+    std::vector<WinDesc> d;
+    size_t smem = 0;
+    if (!window_descs<R>(ss, order, o, bestC, d, smem, err)) return MCBA_ERR_INVALID;
+    CK(cudaMemcpyAsync(pb.desc.p, d.data(), d.size() * sizeof(WinDesc), cudaMemcpyHostToDevice, stm));
+    window_clusters<R>(bestC, smem);
+    cudaGraph_t tmp;
+    CK(cudaStreamBeginCapture(stm, cudaStreamCaptureModeRelaxed));
+    cudaMemsetAsync(pb.queue.p, 0, sizeof(int), stm);
+    launch_windows<R>(pb, n, o, bestC, bestN, bestSmem, stm);
+    CK(cudaStreamEndCapture(stm, &tmp));
+    pb.g = tmp;
+    CK(cudaGraphInstantiate(&pb.ge, pb.g, 0));
+    pb.uids = uids;
+    pb.gens = gens;
+    pb.logs = logs;
+    pb.iters = o.iterations;
+    pb.trials = o.max_trials;
+    pb.tau = o.tau;
+    pb.device = s0->device;
+    pb.precision = s0->precision;
+    pb.C = bestC;
+    pb.nclusters = bestN;
+    pb.smem = bestSmem;
+  }
+  CK(cudaEventRecord(s0->ev[0], stm));
+  CK(cudaGraphLaunch(pb.ge, stm));
+  CK(cudaEventRecord(s0->ev[1], stm));
+  for (int i = 0; i < n; ++i) {
+    CK(cudaMemcpyAsync(ss[i]->lm_host, ss[i]->lm.p, sizeof(LMState), cudaMemcpyDeviceToHost, stm));
+    outs[i].d2h += sizeof(LMState);
+  }
+  CK(cudaStreamSynchronize(stm));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, s0->ev[0], s0->ev[1]);
+  if (ms_device) *ms_device = ms;
+  if (cluster_ctas) *cluster_ctas = pb.C;
+  for (int i = 0; i < n; ++i) {
+    Solver* s = ss[i];
+    SolveResult& out = outs[i];
+    out.ms_total = ms;
+    out.iterations = s->lm_host->iteration;
+    out.launches += (i == 0) ? 1 : 0;  // one kernel for the whole batch
+    const int r = finish_run<R>(s, o, out, err);
+    if (r) return r;
+  }
+  return MCBA_OK;
+}
+}  // namespace
+
+int solver_run_batch_persistent(Solver* const* ss, int n, const RunOptions& o, SolveResult* outs, double* ms_device,
+                                int* cluster_ctas, std::string* err) {
+  if (n <= 0) return MCBA_OK;
+  for (int i = 0; i < n; ++i) {
+    if (!ss[i] || !ss[i]->uploaded) {
+      if (err) *err = "every problem of the batch must be prepared";
+      return MCBA_ERR_INVALID;
+    }
+    if (ss[i]->device != ss[0]->device || ss[i]->precision != ss[0]->precision) {
+      if (err) *err = "the problems of one persistent batch must share a device and a precision";
+      return MCBA_ERR_INVALID;
+    }
+  }
+  CK(cudaSetDevice(ss[0]->device));
+  const int max_log = std::max(1, o.iterations * o.max_trials);
+  for (int i = 0; i < n; ++i) CK(ss[i]->log.ensure(max_log));
+  std::lock_guard<std::mutex> lk(g_pbatch_mu);
+  return ss[0]->precision == MCBA_PREC_MIXED ? run_windows<float>(ss, n, o, outs, ms_device, cluster_ctas, err)
+                                             : run_windows<double>(ss, n, o, outs, ms_device, cluster_ctas, err);
 }
 
 int solver_run(Solver* s, const RunOptions& o, bool restore, SolveResult& out, std::string* err) {

@@ -74,3 +74,68 @@ def test_local_ba_windows_in_one_launch_equal_single_solves(precision, gpu):
                 np.testing.assert_array_equal(s.trial_log(), log)
                 np.testing.assert_array_equal(bqt, qt)
                 np.testing.assert_array_equal(bX, X)
+
+
+def _persistent_windows():
+    """Uneven windows for the persistent launch: small and large reduced
+    systems (5 to 40 keyframes: 1 to 15 tile rows of the cluster
+    factorisation), a window with every pose fixed (no reduced system) and
+    one with every point fixed (no point blocks)."""
+    wins = synth.window_batch(5, seed=91, kf_range=(5, 40), pts_per_kf=(40, 90))
+    pts_only = synth.config(1)
+    pts_only.pose_fixed[:] = 1
+    poses_only = synth.local_ba(8, 600, 93, name="poses_only")
+    poses_only.point_fixed[:] = 1
+    big = synth.local_ba(40, 1600, 95, corridor=True, name="window_40kf")
+    return wins + [pts_only, poses_only, big]
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_persistent_window_launch_equals_single_solves(precision, gpu):
+    """One persistent launch for all windows (clusters take windows from a
+    device queue) gives every window's single solve bit for bit: the trial
+    log, the final cost and the estimates.  The autotuner's first call runs
+    the batch at every cluster size it tries, so the equality also holds
+    across cluster sizes.  In FP64 the single solves follow the oracle trial
+    by trial; one window is checked against the oracle here as well."""
+    wins = _persistent_windows()
+    iters = 6
+    single = []
+    for pr in wins:
+        with ba.Solver(precision=precision) as s:
+            s.load(pr)
+            st = s.optimize(iters)
+            single.append((st, s.trial_log(), s.state()))
+    with ba.LocalBABatch(wins, precision=precision) as b:
+        for rep in range(2):  # the second call reuses the tuned, captured launch
+            stats, ms = b.solve(iters, persistent=True)
+            assert ms > 0 and b.cluster_ctas in (4, 8, 16)
+            assert sum(st["kernel_launches"] for st in stats) == 1
+            states = b.states()
+            for (st, log, (qt, X)), bst, (bqt, bX), s in zip(single, stats, states, b.solvers):
+                assert bst["final_chi2"] == st["final_chi2"]
+                assert bst["iterations"] == st["iterations"] and bst["trials"] == st["trials"]
+                np.testing.assert_array_equal(s.trial_log(), log)
+                np.testing.assert_array_equal(bqt, qt)
+                np.testing.assert_array_equal(bX, X)
+    if precision == "fp64":
+        o = oracle.optimize(wins[-1], iters)
+        g = single[-1][1]
+        assert len(g) == len(o["log"])
+        for a, r in zip(g, o["log"]):
+            assert a["accepted"] == r["accepted"]
+            assert abs(a["chi_after"] - r["chi_after"]) <= 1e-9 * abs(r["chi_after"])
+
+
+def test_persistent_window_launch_rejects_oversize_windows(gpu):
+    """A window whose reduced system exceeds 384 unknowns is refused with
+    MCBA_ERR_INVALID (no launch); the graph-branch batch solves it."""
+    from mcvslam_gb300 import _native as N
+
+    big = synth.local_ba(70, 3000, 97, corridor=True, name="window_70kf")
+    small = synth.window_batch(1, seed=98, kf_range=(5, 6), pts_per_kf=(50, 60))[0]
+    with ba.LocalBABatch([small, big], precision="mixed") as b:
+        with pytest.raises(N.MCBAError):
+            b.solve(2, persistent=True)
+        stats, ms = b.solve(2)  # the graph-branch batch still solves it
+        assert all(np.isfinite(st["final_chi2"]) for st in stats)

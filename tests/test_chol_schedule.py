@@ -1,5 +1,5 @@
 """CPU emulation of the dataflow schedule of the cluster LDL^T
-(mcvslam_gb300/csrc/mcba_chol.cu): the per-CTA task lists of worker_tasks(),
+(mcvslam_gb300/csrc/mcba_chol_dev.cuh): the per-CTA task lists of worker_tasks(),
 the version-flag conditions of load_task() and of the chain CTA, and the
 tile-major workspace.  The CTAs step in random interleavings, each task runs
 only when its flags say its inputs are ready, and the test checks that
