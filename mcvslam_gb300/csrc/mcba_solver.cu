@@ -118,6 +118,7 @@ struct Bufs {
   double* x;        // [6Kf + 3Lf]
   double* cost_part;
   double* scale_part;
+  int* done;  // [2] CTAs finished in k_cost_step / k_reduce (0 between launches)
   LMState* lm;
   mcba_trial_log* log;
 };
@@ -160,6 +161,16 @@ __device__ __forceinline__ void load_row<double, 20>(const double* p, double* v)
   const double2* q = reinterpret_cast<const double2*>(p);
 #pragma unroll
   for (int i = 0; i < 10; ++i) {
+    const double2 t = q[i];
+    v[2 * i] = t.x;
+    v[2 * i + 1] = t.y;
+  }
+}
+template <>
+__device__ __forceinline__ void load_row<double, 10>(const double* p, double* v) {
+  const double2* q = reinterpret_cast<const double2*>(p);
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
     const double2 t = q[i];
     v[2 * i] = t.x;
     v[2 * i + 1] = t.y;
@@ -290,6 +301,12 @@ __device__ __forceinline__ T blk_sum(T x, T* sh, const Blk& b) {
   return r;
 }
 
+// Start of one LM iteration (the trial loop's state).
+__device__ __forceinline__ void iter_begin(LMState* lm) {
+  lm->trial = 0;
+  lm->trial_continue = 1;
+}
+
 __device__ __forceinline__ void pose_lin_one(const double* q, PoseLinD* pd, PoseLinF* pf) {
   double Rm[9];
   quat_to_R(q, Rm);
@@ -412,9 +429,17 @@ __device__ __forceinline__ void linearize_blk(const Bufs& B, const Blk& b, Acc<R
   }
 }
 
+// The first kernel of an LM iteration: its first thread also starts the
+// iteration (trial count, trial loop armed; in a graph it re-arms the trial
+// loop's condition, whose default applies only when the whole graph is
+// launched).
 template <typename R>
-__global__ void __launch_bounds__(kLinThreads) k_linearize(Bufs B) {
+__global__ void __launch_bounds__(kLinThreads) k_linearize(Bufs B, cudaGraphConditionalHandle h_trial, int in_graph) {
   __shared__ Acc<R> sh[kLinThreads / 32][32];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    iter_begin(B.lm);
+    if (in_graph) cudaGraphSetConditional(h_trial, 1u);
+  }
   linearize_blk<R>(B, grid_blk(), sh);
 }
 
@@ -478,13 +503,34 @@ __device__ __forceinline__ void point_reduce_thread(const Bufs& B, int Lf, int l
 #pragma unroll 4
   for (int e = e0; e < e1; ++e) {
     const R* row = Ptrs<R>::p(B.rows) + (size_t)e * row_stride<R>();
+    // the row's Hll, b_l (and low halves) by 16-byte loads: entries 16..35
+    // of an FP32 row, 18..27 of an FP64 row
+    R hv[6], bv[3], lov[6];
+    if constexpr (row_stride<R>() > kHllLo) {
+      R t[20];
+      load_row<R, 20>(row + 16, t);
 #pragma unroll
-    for (int k = 0; k < 6; ++k) {
-      h[k].add(row[18 + k]);
-      if constexpr (row_stride<R>() > kHllLo) h[k].lo = __fadd_rn(h[k].lo, row[kHllLo + k]);
+      for (int k = 0; k < 6; ++k) {
+        hv[k] = t[2 + k];
+        lov[k] = t[kHllLo - 16 + k];
+      }
+#pragma unroll
+      for (int k = 0; k < 3; ++k) bv[k] = t[8 + k];
+    } else {
+      R t[10];
+      load_row<R, 10>(row + 18, t);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) hv[k] = t[k];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) bv[k] = t[6 + k];
     }
 #pragma unroll
-    for (int k = 0; k < 3; ++k) s[k] += row[24 + k];
+    for (int k = 0; k < 6; ++k) {
+      h[k].add(hv[k]);
+      if constexpr (row_stride<R>() > kHllLo) h[k].lo = __fadd_rn(h[k].lo, lov[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) s[k] += bv[k];
   }
   double* H = B.Hll + (size_t)l * 6;
 #pragma unroll
@@ -496,14 +542,7 @@ __device__ __forceinline__ void point_reduce_thread(const Bufs& B, int Lf, int l
 
 // Both reductions in one launch of 128-thread blocks: the first blocks take
 // four free poses each (a warp per pose), the rest 128 free points each.
-template <typename R>
-__global__ void k_reduce(Bufs B, int Kf, int Lf, int npose_blocks) {
-  const int blk = blockIdx.x;
-  if (blk < npose_blocks)
-    pose_reduce_warp<R>(B, Kf, 4 * blk + (threadIdx.x >> 5), threadIdx.x & 31);
-  else
-    point_reduce_thread<R>(B, Lf, (blk - npose_blocks) * blockDim.x + threadIdx.x);
-}
+
 
 // computeLambdaInit (optimization_algorithm_levenberg.cpp:145-157):
 // tau * max |H_jj| over every free vertex (poses and points): a grid-wide
@@ -538,20 +577,6 @@ __device__ __forceinline__ unsigned long long lambda_max_part(const Bufs& B, int
   return m;
 }
 
-template <typename R>
-__global__ void k_lambda_max(Bufs B, int Kf, int Lf) {
-  __shared__ unsigned long long sh[32];
-  if (B.lm->iteration != 0) return;
-  const unsigned long long m =
-      lambda_max_part<R>(B, Kf, Lf, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned long long r = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = sh[w] > r ? sh[w] : r;
-    atomicMax(&B.lm->lam_bits, r);
-  }
-}
 
 __device__ __forceinline__ void lambda_set(LMState* lm, double tau) {
   if (lm->iteration != 0) return;
@@ -559,7 +584,57 @@ __device__ __forceinline__ void lambda_set(LMState* lm, double tau) {
   lm->ni = 2.0;
 }
 
-__global__ void k_lambda_set(LMState* lm, double tau) { lambda_set(lm, tau); }
+// Both reductions in one launch of 128-thread blocks: the first blocks take
+// four free poses each (a warp per pose), the rest 128 free points each.  In
+// the first iteration the launch also forms computeLambdaInit's maximum
+// (every block's maximum of its diagonal entries into lam_bits), and the
+// last block to finish sets lambda from it.
+template <typename R>
+__global__ void k_reduce(Bufs B, int Kf, int Lf, int npose_blocks, double tau) {
+  __shared__ int s_last;
+  const int blk = blockIdx.x;
+  const int lane = threadIdx.x & 31;
+  int idx;
+  if (blk < npose_blocks) {
+    idx = 4 * blk + (threadIdx.x >> 5);
+    pose_reduce_warp<R>(B, Kf, idx, lane);
+  } else {
+    idx = (blk - npose_blocks) * blockDim.x + threadIdx.x;
+    point_reduce_thread<R>(B, Lf, idx);
+  }
+  if (B.lm->iteration != 0) return;
+  // the diagonal entries this thread stored (Hpp's diagonal on the pose
+  // warps' lanes 0, 6, 11, 15, 18, 20; Hll's three for a point's thread)
+  unsigned long long m = 0;
+  if (blk < npose_blocks) {
+    if (idx < Kf && (lane == 0 || lane == 6 || lane == 11 || lane == 15 || lane == 18 || lane == 20)) {
+      const int r = lane == 0 ? 0 : lane == 6 ? 1 : lane == 11 ? 2 : lane == 15 ? 3 : lane == 18 ? 4 : 5;
+      m = abs_bits(B.Hpp[(size_t)idx * 36 + 7 * r]);
+    }
+  } else if (idx < Lf) {
+    const double* H = B.Hll + (size_t)idx * 6;
+    const unsigned long long a = abs_bits(H[0]), b = abs_bits(H[3]), c = abs_bits(H[5]);
+    m = a > b ? a : b;
+    m = c > m ? c : m;
+  }
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    const unsigned long long v = __shfl_xor_sync(0xffffffffu, m, o);
+    m = v > m ? v : m;
+  }
+  if (lane == 0 && m) atomicMax(&B.lm->lam_bits, m);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(&B.done[1], 1) == (int)gridDim.x - 1;
+  }
+  __syncthreads();
+  if (s_last && threadIdx.x == 0) {
+    __threadfence();
+    B.done[1] = 0;
+    lambda_set(B.lm, tau);
+  }
+}
 
 template <typename R>
 __device__ __forceinline__ void damped_inverse(const R* Hu, R lam, R* Di) {
@@ -789,7 +864,8 @@ __device__ __forceinline__ void backsub_block(const Bufs& B, int Lf, int n, int 
     for (int e = B.pt_begin[l] + sub; e < e1; e += kPtLanes) {
       const int ph = B.canon_pose_h[e];
       if (ph < 0) continue;
-      const R* H = Ptrs<R>::p(B.rows) + (size_t)e * row_stride<R>();
+      R H[20];
+      load_row<R, 20>(Ptrs<R>::p(B.rows) + (size_t)e * row_stride<R>(), H);
       const double* xp = B.x + 6 * (size_t)ph;
       R xr[6];
 #pragma unroll
@@ -920,11 +996,7 @@ __device__ __forceinline__ void cost_blk(const Bufs& B, const Blk& b, int E, int
   }
 }
 
-template <typename R>
-__global__ void __launch_bounds__(256) k_cost(Bufs B, int E, int which) {
-  __shared__ double sh[32];
-  cost_blk<R>(B, grid_blk(), E, which, sh);
-}
+
 
 __device__ __forceinline__ void lm_begin_blk(const Bufs& B, const Blk& b, int ncost, double* sh) {
   double s = 0.0;
@@ -936,10 +1008,7 @@ __device__ __forceinline__ void lm_begin_blk(const Bufs& B, const Blk& b, int nc
   }
 }
 
-__global__ void k_lm_begin(Bufs B, int ncost) {
-  __shared__ double sh[32];
-  lm_begin_blk(B, grid_blk(), ncost, sh);
-}
+
 
 // One LM trial's decision (optimization_algorithm_levenberg.cpp:113-141).
 // The two partial sums run side by side (each in the order and tree of
@@ -1032,10 +1101,32 @@ __device__ __forceinline__ int lm_decide_blk(const Bufs& B, const Blk& b, int nc
   return more ? 1 : 0;
 }
 
-__global__ void k_lm_decide(Bufs B, int ncost, int nscale, cudaGraphConditionalHandle h_trial, int in_graph) {
+// activeRobustChi2 of the current (which = 0) or candidate (which = 1)
+// state, one partial per CTA; the last CTA to finish then sums the partials
+// (the fixed order and tree of a one-block launch) and takes the LM step:
+// the initial cost (which = 0), or the trial's decision (which = 1), which
+// in a graph also sets the trial loop's condition.
+template <typename R>
+__global__ void __launch_bounds__(256) k_cost_step(Bufs B, int E, int which, int nscale,
+                                                   cudaGraphConditionalHandle h_trial, int in_graph) {
   __shared__ double sh[64];
-  const int more = lm_decide_blk(B, grid_blk(), ncost, nscale, sh);
-  if (more >= 0 && in_graph) cudaGraphSetConditional(h_trial, more ? 1u : 0u);
+  __shared__ int s_last;
+  cost_blk<R>(B, grid_blk(), E, which, sh);
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(&B.done[0], 1) == (int)gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  if (threadIdx.x == 0) B.done[0] = 0;
+  const Blk b{0, (int)threadIdx.x, (int)blockDim.x, 0};
+  if (which == 0) {
+    lm_begin_blk(B, b, (int)gridDim.x, sh);
+  } else {
+    const int more = lm_decide_blk(B, b, (int)gridDim.x, nscale, sh);
+    if (more >= 0 && in_graph) cudaGraphSetConditional(h_trial, more ? 1u : 0u);
+  }
 }
 
 // LM state at the start of a solve (OptimizationAlgorithmLevenberg members
@@ -1076,17 +1167,7 @@ __global__ void k_iter_end(LMState* lm, cudaGraphConditionalHandle h_iter) {
 // trial loop: a conditional handle's default value is applied only when the
 // whole graph is launched, so without this the inner WHILE would run zero
 // times from the second iteration on.
-__device__ __forceinline__ void iter_begin(LMState* lm) {
-  lm->trial = 0;
-  lm->trial_continue = 1;
-}
 
-__global__ void k_iter_begin(LMState* lm, cudaGraphConditionalHandle h_trial, int in_graph) {
-  if (threadIdx.x == 0) {
-    iter_begin(lm);
-    if (in_graph) cudaGraphSetConditional(h_trial, 1u);
-  }
-}
 
 // Zero the reduced camera matrix storage and put ones on the padding diagonal.
 __device__ __forceinline__ void init_S_range(double* S, int ld, int n, size_t total, size_t i0, size_t step) {
@@ -1314,6 +1395,7 @@ class Solver {
   // numerics
   DBuf<char> rows, partials, Hll, bl, pdv, yq, ppart, qpart;
   DBuf<double> Hpp, bp, S, cws, dinv, x, cost_part, scale_part, chi2_out;
+  DBuf<int> done;
   DBuf<LMState> lm;
   DBuf<mcba_trial_log> log;
   LMState* lm_host = nullptr;
@@ -1377,7 +1459,7 @@ class Solver {
     obs_all.release();
     DBuf<int>* is[] = {&chunk_begin, &chunk_pose, &pose_chunk_begin, &pt_begin, &canon_pose_h, &canon_point_h,
                        &pchunk_begin, &block_ab, &block_chunk_begin, &pose_canon_begin, &pose_canon_list,
-                       &free_pose_ids, &free_point_ids};
+                       &free_pose_ids, &free_point_ids, &done};
     for (auto* d : is) d->release();
     pairs.release();
     DBuf<char>* cs[] = {&rows, &partials, &Hll, &bl, &pdv, &yq, &ppart, &qpart};
@@ -1635,6 +1717,7 @@ Bufs make_bufs(Solver* s) {
   B.x = s->x.p;
   B.cost_part = s->cost_part.p;
   B.scale_part = s->scale_part.p;
+  B.done = s->done.p;
   B.lm = s->lm.p;
   B.log = s->log.p;
   return B;
@@ -1676,23 +1759,18 @@ struct PhaseClock {
 };
 
 template <typename R>
-void launch_linearize(Solver* s, const Bufs& B, const Launch& L, bool first, double tau, PhaseClock& pc) {
+void launch_linearize(Solver* s, const Bufs& B, const Launch& L, double tau, PhaseClock& pc,
+                      cudaGraphConditionalHandle h_trial, int in_graph) {
   cudaStream_t st = s->stream;
   pc.run(MCBA_PHASE_LINEARIZE, [&] {
-    k_linearize<R><<<L.nchunk, kLinThreads, 0, st>>>(B);
+    k_linearize<R><<<L.nchunk, kLinThreads, 0, st>>>(B, h_trial, in_graph);
     s->launches++;
   });
   pc.run(MCBA_PHASE_REDUCE, [&] {
     if (L.Kf || L.Lf) {
       const int npb = (L.Kf + 3) / 4;
-      k_reduce<R><<<npb + (L.Lf + 127) / 128, 128, 0, st>>>(B, L.Kf, L.Lf, npb);
+      k_reduce<R><<<npb + (L.Lf + 127) / 128, 128, 0, st>>>(B, L.Kf, L.Lf, npb, tau);
       s->launches++;
-    }
-    if (first) {
-      const int nv = 6 * L.Kf + 3 * L.Lf;
-      k_lambda_max<R><<<std::max(1, std::min((nv + 255) / 256, 304)), 256, 0, st>>>(B, L.Kf, L.Lf);
-      k_lambda_set<<<1, 1, 0, st>>>(B.lm, tau);
-      s->launches += 2;
     }
   });
 }
@@ -1744,9 +1822,8 @@ void launch_trial(Solver* s, const Bufs& B, const Launch& L, PhaseClock& pc, cud
     s->launches += 1;
   });
   pc.run(MCBA_PHASE_COST, [&] {
-    k_cost<R><<<L.ncost, 256, 0, st>>>(B, L.E, 1);
-    k_lm_decide<<<1, 256, 0, st>>>(B, L.ncost, L.nscale_pts + L.nscale_pose, h_trial, in_graph);
-    s->launches += 2;
+    k_cost_step<R><<<L.ncost, 256, 0, st>>>(B, L.E, 1, L.nscale_pts + L.nscale_pose, h_trial, in_graph);
+    s->launches += 1;
   });
 }
 
@@ -1772,6 +1849,7 @@ int alloc_numerics(Solver* s, std::string* err) {
   CK(s->x.ensure(std::max(nx, 1)));
   CK(s->cost_part.ensure(L.ncost));
   CK(s->scale_part.ensure(L.nscale_pts + L.nscale_pose));
+  CK(s->done.ensure(2));
   CK(s->lm.ensure(1));
   return MCBA_OK;
 }
@@ -1792,10 +1870,10 @@ int launch_prologue(Solver* s, const Bufs& B, const RunOptions& o, bool restore,
   const size_t total = (size_t)(L.ld + kNB) * L.ld;
   k_init_S<<<(int)std::min<size_t>((total + 255) / 256, 4096), 256, 0, st>>>(B.S, L.ld, L.n, total);
   CK(cudaMemsetAsync(B.x, 0, std::max(nx, 1) * sizeof(double), st));
+  CK(cudaMemsetAsync(B.done, 0, 2 * sizeof(int), st));
   k_lm_reset<<<1, 1, 0, st>>>(B.lm, o.max_trials, max_log, o.iterations, h_iter, in_graph);
-  k_cost<R><<<L.ncost, 256, 0, st>>>(B, L.E, 0);
-  k_lm_begin<<<1, 256, 0, st>>>(B, L.ncost);
-  s->launches += 4;
+  k_cost_step<R><<<L.ncost, 256, 0, st>>>(B, L.E, 0, 0, 0, 0);
+  s->launches += 3;
   CK(cudaGetLastError());
   return MCBA_OK;
 }
@@ -1853,9 +1931,7 @@ int add_lm_subgraph(Solver* s, cudaGraph_t G, const RunOptions& o, bool restore,
 
   const int64_t l1 = s->launches;
   CK(cudaStreamBeginCaptureToGraph(st, body_it, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-  k_iter_begin<<<1, 32, 0, st>>>(B.lm, h_trial, 1);
-  s->launches++;
-  launch_linearize<R>(s, B, L, true, o.tau, pc);
+  launch_linearize<R>(s, B, L, o.tau, pc, h_trial, 1);
   r = capture_leaves(st, leaves, err);
   CK(cudaStreamEndCapture(st, &tmp));
   if (r) return r;
@@ -1972,10 +2048,8 @@ int run_lm(Solver* s, const RunOptions& o, bool restore, SolveResult& out, std::
   int it = 0;
   bool stop = false;
   for (it = 0; it < iterations && !stop; ++it) {
-    k_iter_begin<<<1, 32, 0, stm>>>(B.lm, 0, 0);
-    s->launches++;
     CK(cudaEventRecord(s->ev[2], stm));
-    launch_linearize<R>(s, B, L, it == 0, o.tau, pc);
+    launch_linearize<R>(s, B, L, o.tau, pc, 0, 0);
     CK(cudaEventRecord(s->ev[3], stm));
     for (int t = 0; t < max_trials; ++t) {
       launch_trial<R>(s, B, L, pc, 0, 0);
