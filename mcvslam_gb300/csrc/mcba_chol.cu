@@ -17,6 +17,8 @@ using namespace chold;
 __global__ void __launch_bounds__(kThreads, 1) k_ldlt_cluster(const double* S, double* ws, double* x,
                                                               int* solve_ok, Geo g) {
   extern __shared__ __align__(16) double sm[];
+  // launched as a programmatic dependent of the Schur assembly: wait for it
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   ldlt_cluster_run(S, ws, x, solve_ok, g, sm);
 }
 
@@ -85,13 +87,15 @@ cudaError_t chol_cluster_launch(const CholPlan& plan, const double* S, double* w
   cfg.blockDim = dim3(kThreads, 1, 1);
   cfg.dynamicSmemBytes = plan.smem_bytes;
   cfg.stream = st;
-  cudaLaunchAttribute attr;
-  attr.id = cudaLaunchAttributeClusterDimension;
-  attr.val.clusterDim.x = plan.cluster;
-  attr.val.clusterDim.y = 1;
-  attr.val.clusterDim.z = 1;
-  cfg.attrs = &attr;
-  cfg.numAttrs = 1;
+  cudaLaunchAttribute attr[2];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = plan.cluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[1].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 2;
   return cudaLaunchKernelEx(&cfg, k_ldlt_cluster, S, ws, x, solve_ok, g);
 }
 

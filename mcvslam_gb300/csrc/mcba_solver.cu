@@ -288,6 +288,12 @@ struct Blk {
 };
 __device__ __forceinline__ Blk grid_blk() { return Blk{(int)blockIdx.x, (int)threadIdx.x, (int)blockDim.x, 0}; }
 
+// The kernels of the LM chain are launched with programmatic stream
+// serialisation: a kernel's launch overlaps the end of the one before it,
+// and its first instruction waits until that grid has completed and its
+// writes are visible (a no-op for a plain launch).
+__device__ __forceinline__ void chain_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // block_sum over a Blk (same tree as dev::block_sum for the same block size)
 template <typename T>
 __device__ __forceinline__ T blk_sum(T x, T* sh, const Blk& b) {
@@ -436,6 +442,7 @@ __device__ __forceinline__ void linearize_blk(const Bufs& B, const Blk& b, Acc<R
 template <typename R>
 __global__ void __launch_bounds__(kLinThreads) k_linearize(Bufs B, cudaGraphConditionalHandle h_trial, int in_graph) {
   __shared__ Acc<R> sh[kLinThreads / 32][32];
+  chain_wait();
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     iter_begin(B.lm);
     if (in_graph) cudaGraphSetConditional(h_trial, 1u);
@@ -592,6 +599,7 @@ __device__ __forceinline__ void lambda_set(LMState* lm, double tau) {
 template <typename R>
 __global__ void k_reduce(Bufs B, int Kf, int Lf, int npose_blocks, double tau) {
   __shared__ int s_last;
+  chain_wait();
   const int blk = blockIdx.x;
   const int lane = threadIdx.x & 31;
   int idx;
@@ -675,6 +683,7 @@ __device__ __forceinline__ void point_dinv_one(const Bufs& B, int l) {
 
 template <typename R>
 __global__ void __launch_bounds__(128) k_point_dinv(Bufs B, int Lf) {
+  chain_wait();
   const int l = blockIdx.x * blockDim.x + threadIdx.x;
   if (l < Lf) point_dinv_one<R>(B, l);
 }
@@ -734,6 +743,7 @@ __device__ __forceinline__ void schur_edge_blk(const Bufs& B, const Blk& b, Acc<
 template <typename R>
 __global__ void __launch_bounds__(kLinThreads) k_schur_edge(Bufs B) {
   __shared__ Acc<R> sh[6][kLinThreads / 32];
+  chain_wait();
   schur_edge_blk<R>(B, grid_blk(), sh);
 }
 
@@ -781,6 +791,7 @@ __device__ __forceinline__ void schur_pairs_warp(const Bufs& B, int warp, int la
 
 template <typename R>
 __global__ void __launch_bounds__(256) k_schur_pairs(Bufs B, int npc) {
+  chain_wait();
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (warp < npc) schur_pairs_warp<R>(B, warp, threadIdx.x & 31);
 }
@@ -837,6 +848,7 @@ __device__ __forceinline__ void schur_assemble_blk(const Bufs& B, const Blk& b, 
 template <typename R>
 __global__ void __launch_bounds__(64 * kAsmGroups) k_schur_assemble(Bufs B, int ld) {
   __shared__ Acc<R> sh[kAsmGroups][36];
+  chain_wait();
   schur_assemble_blk<R>(B, grid_blk(), ld, sh);
 }
 
@@ -962,6 +974,7 @@ __device__ __forceinline__ void update_blk(const Bufs& B, const Blk& b, int Lf, 
 template <typename R>
 __global__ void k_update(Bufs B, int Lf, int n, int Kf, int npose_blocks, int npt_blocks) {
   __shared__ double sh[32];
+  chain_wait();
   update_blk<R>(B, grid_blk(), Lf, n, Kf, npose_blocks, npt_blocks, sh);
 }
 
@@ -1111,6 +1124,7 @@ __global__ void __launch_bounds__(256) k_cost_step(Bufs B, int E, int which, int
                                                    cudaGraphConditionalHandle h_trial, int in_graph) {
   __shared__ double sh[64];
   __shared__ int s_last;
+  chain_wait();
   cost_blk<R>(B, grid_blk(), E, which, sh);
   if (threadIdx.x == 0) {
     __threadfence();
@@ -1758,18 +1772,34 @@ struct PhaseClock {
   }
 };
 
+// A kernel of the LM chain, launched so that it may start while the kernel
+// before it on the stream finishes (see chain_wait).
+template <typename... KArgs, typename... Args>
+void launch_chain(void (*k)(KArgs...), int grid, int block, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid, 1, 1);
+  cfg.blockDim = dim3((unsigned)block, 1, 1);
+  cfg.stream = st;
+  cudaLaunchAttribute at;
+  at.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at.val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = &at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k, static_cast<KArgs>(args)...);
+}
+
 template <typename R>
 void launch_linearize(Solver* s, const Bufs& B, const Launch& L, double tau, PhaseClock& pc,
                       cudaGraphConditionalHandle h_trial, int in_graph) {
   cudaStream_t st = s->stream;
   pc.run(MCBA_PHASE_LINEARIZE, [&] {
-    k_linearize<R><<<L.nchunk, kLinThreads, 0, st>>>(B, h_trial, in_graph);
+    launch_chain(k_linearize<R>, L.nchunk, kLinThreads, st, B, h_trial, in_graph);
     s->launches++;
   });
   pc.run(MCBA_PHASE_REDUCE, [&] {
     if (L.Kf || L.Lf) {
       const int npb = (L.Kf + 3) / 4;
-      k_reduce<R><<<npb + (L.Lf + 127) / 128, 128, 0, st>>>(B, L.Kf, L.Lf, npb, tau);
+      launch_chain(k_reduce<R>, npb + (L.Lf + 127) / 128, 128, st, B, L.Kf, L.Lf, npb, tau);
       s->launches++;
     }
   });
@@ -1781,23 +1811,23 @@ void launch_trial(Solver* s, const Bufs& B, const Launch& L, PhaseClock& pc, cud
   cudaStream_t st = s->stream;
   if (L.Lf) {
     pc.run(MCBA_PHASE_SCHUR_EDGE, [&] {
-      k_point_dinv<R><<<(L.Lf + 127) / 128, 128, 0, st>>>(B, L.Lf);
+      launch_chain(k_point_dinv<R>, (L.Lf + 127) / 128, 128, st, B, L.Lf);
       s->launches++;
     });
   }
   if (L.Kf) {
     pc.run(MCBA_PHASE_SCHUR_EDGE, [&] {
-      k_schur_edge<R><<<L.nchunk, kLinThreads, 0, st>>>(B);
+      launch_chain(k_schur_edge<R>, L.nchunk, kLinThreads, st, B);
       s->launches++;
     });
     pc.run(MCBA_PHASE_SCHUR_PAIRS, [&] {
       if (L.npc) {
-        k_schur_pairs<R><<<(L.npc + 7) / 8, 256, 0, st>>>(B, L.npc);
+        launch_chain(k_schur_pairs<R>, (L.npc + 7) / 8, 256, st, B, L.npc);
         s->launches++;
       }
     });
     pc.run(MCBA_PHASE_SCHUR_ASSEMBLE, [&] {
-      k_schur_assemble<R><<<L.nblk, 64 * kAsmGroups, 0, st>>>(B, L.ld);
+      launch_chain(k_schur_assemble<R>, L.nblk, 64 * kAsmGroups, st, B, L.ld);
       s->launches++;
     });
     pc.run(MCBA_PHASE_CHOLESKY, [&] {
@@ -1818,11 +1848,11 @@ void launch_trial(Solver* s, const Bufs& B, const Launch& L, PhaseClock& pc, cud
     });
   }
   pc.run(MCBA_PHASE_UPDATE, [&] {
-    k_update<R><<<L.nscale_pose + L.nscale_pts, 128, 0, st>>>(B, L.Lf, L.n, L.Kf, L.nscale_pose, L.nscale_pts);
+    launch_chain(k_update<R>, L.nscale_pose + L.nscale_pts, 128, st, B, L.Lf, L.n, L.Kf, L.nscale_pose, L.nscale_pts);
     s->launches += 1;
   });
   pc.run(MCBA_PHASE_COST, [&] {
-    k_cost_step<R><<<L.ncost, 256, 0, st>>>(B, L.E, 1, L.nscale_pts + L.nscale_pose, h_trial, in_graph);
+    launch_chain(k_cost_step<R>, L.ncost, 256, st, B, L.E, 1, L.nscale_pts + L.nscale_pose, h_trial, in_graph);
     s->launches += 1;
   });
 }
