@@ -72,6 +72,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--windows", type=int, default=64,
+                    help="local-BA windows of --config 4 (64 is the benchmark; fewer for a profiler capture)")
     ap.add_argument("--workload", default="ba", choices=["ba", "knn", "project", "stereo"],
                     help="ba: the local-BA solve (default); knn: brute-force Hamming k=2 matching; "
                          "project: map-point projection + windowed match over a batch of objects; "
@@ -558,7 +560,7 @@ def run_config4(args):
     torch.cuda.set_device(local)
     iters = LBA_ITERS[2]
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
-    wins = synth.window_batch(64)
+    wins = synth.window_batch(args.windows)
     rng = np.random.default_rng(4100)
     frames = [synth.pose_only(int(rng.integers(500, 6001)), seed=4200 + i) for i in range(256)]
     clocks = ClockSampler(local)
@@ -607,7 +609,7 @@ def run_config4(args):
     gaps = np.array(gaps)
     # end to end through the C ABI with host buffers
     e2e_ms, pe2e_ms = [], []
-    for i in range(args.warmup + args.steps):
+    for i in range(0 if args.no_e2e else args.warmup + args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         with ba.LocalBABatch(wins, precision="mixed", device=local) as b2:
@@ -675,10 +677,11 @@ def run_config4(args):
                        "pose_only_frames": len(frames), "pose_only_edges": int(sum(f.n_edges for f in frames)),
                        "pose_only_ms": p_ms, "pose_only_frames_per_s": len(frames) / (p_ms / 1e3),
                        "l2": "flushed (256 MB write) before every step"},
-            "e2e": {"value": edges / (statistics.mean(e2e_ms) / 1e3), "unit": "edges/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "ms_per_step": statistics.mean(e2e_ms),
-                    "pose_only_ms": statistics.mean(pe2e_ms),
-                    "pose_only_frames_per_s": len(frames) / (statistics.mean(pe2e_ms) / 1e3)},
+            "e2e": None if not e2e_ms else {
+                "value": edges / (statistics.mean(e2e_ms) / 1e3), "unit": "edges/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": statistics.mean(e2e_ms),
+                "pose_only_ms": statistics.mean(pe2e_ms),
+                "pose_only_frames_per_s": len(frames) / (statistics.mean(pe2e_ms) / 1e3)},
             "fp64_plain": {"ms_per_step": f_ms, "value": sum(s["edges_linearized"] for s in fstats) / (f_ms / 1e3)},
             "precision_gap": {"per_window_final_cost_rel": [float(g) for g in gaps],
                               "max_abs": float(np.abs(gaps).max()), "bound": 1e-6,
