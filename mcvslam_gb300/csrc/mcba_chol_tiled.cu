@@ -112,20 +112,25 @@ __global__ void __launch_bounds__(kDiagThreads) k_tchol_diag(const double* __res
   // LDL^T, one barrier per pivot.  At pivot kk the next pivot is
   // d_{kk+1} - w^2 / d_kk with w = T[kk+1][kk], whose square was formed at
   // the previous pivot (by the thread that wrote w), so the chain from one
-  // reciprocal to the next is one FMA and the reciprocal itself; the thread
-  // that forms it also takes its share of the other live entries.  After
-  // pivot kk, column kk below the diagonal holds L_unit[i][kk] d_kk.
+  // reciprocal to the next is one FMA and the reciprocal itself.  Thread 0
+  // runs that chain and nothing else, and no other FP64 work shares its
+  // warp's sub-partition: the other live entries go to warps 1-3 and 5-7
+  // (warp 4 is on warp 0's sub-partition and idles).  After pivot kk,
+  // column kk below the diagonal holds L_unit[i][kk] d_kk.
+  const int warp = tid >> 5;
+  const int wk = (warp == 0 || warp == 4) ? -1 : (warp < 4 ? tid - 32 : tid - 64);  // 0..191
+  constexpr int kWorkers = kDiagThreads - 64;
   for (int kk = 0; kk < kTB - 1; ++kk) {
     const int m = kTB - 1 - kk, live = m * (m + 1) / 2;
     const double inv = dinv[kk];
-    for (int e = tid; e < live; e += kDiagThreads) {
-      const int i = kk + 1 + ta[e], j = kk + 1 + tb[e];
-      if (e == 0) {  // (kk+1, kk+1): the next pivot
-        const double v = fma(-w2[kk], inv, T[i][j]);
-        T[i][j] = v;
-        if (!(v > 0.0)) *solve_ok = 0;  // SimplicialLLT's info() != Success (linear_solver_eigen.h:118-126)
-        dinv[kk + 1] = tchol_recip(v);
-      } else {
+    if (tid == 0) {  // (kk+1, kk+1): the next pivot
+      const double v = fma(-w2[kk], inv, T[kk + 1][kk + 1]);
+      T[kk + 1][kk + 1] = v;
+      if (!(v > 0.0)) *solve_ok = 0;  // SimplicialLLT's info() != Success (linear_solver_eigen.h:118-126)
+      dinv[kk + 1] = tchol_recip(v);
+    } else if (wk >= 0) {
+      for (int e = 1 + wk; e < live; e += kWorkers) {
+        const int i = kk + 1 + ta[e], j = kk + 1 + tb[e];
         const double v = fma(-(T[i][kk] * inv), T[j][kk], T[i][j]);
         T[i][j] = v;
         if (e == 1 && kk + 1 < kTB - 1) w2[kk + 1] = v * v;  // (kk+2, kk+1): w of the next pivot
