@@ -188,9 +188,11 @@ __global__ void __launch_bounds__(kDiagThreads) k_tchol_tinv(double* ws, int ld)
 
 // Rows R in [o + kTB, nrows): row segment a (kTB values of panel k)
 // becomes x with x L_kk^T = a.  One warp per row pair, lane l holding entry
-// l (and l + 32 for 64-wide panels): x_j = a_j / L_jj, then a_m -= x_j L_mj
-// for m > j.  Eight rows per CTA; the two rows of a warp run interleaved.
-// L_kk in dynamic shared memory.
+// l (and l + 32 for 64-wide panels): a_m -= a_j (L_mj / L_jj) for m > j,
+// then x_m = a_m / L_mm once at the end, so the dependent chain per column
+// is one shuffle and one FMA.  Eight rows per CTA; the two rows of a warp
+// run interleaved.  L_kk with its columns scaled by 1 / L_jj in dynamic
+// shared memory.
 constexpr size_t kTrsmSmem = sizeof(double) * kTB * (kTB + 1) + sizeof(double) * kTB;
 
 __global__ void __launch_bounds__(128) k_tchol_trsm(double* S, const double* __restrict__ ws, int ld, int k,
@@ -200,8 +202,9 @@ __global__ void __launch_bounds__(128) k_tchol_trsm(double* S, const double* __r
   double* ri = dsm + kTB * (kTB + 1);
   const int tid = threadIdx.x, o = k * kTB, nt = ld / kTB;
   const double* Lk = ws + ws_L(k);
-  for (int idx = tid; idx < kTB * kTB; idx += 128) Ls[idx / kTB][idx % kTB] = Lk[idx];
   if (tid < kTB) ri[tid] = ws[ws_r(nt) + o + tid];
+  __syncthreads();
+  for (int idx = tid; idx < kTB * kTB; idx += 128) Ls[idx / kTB][idx % kTB] = Lk[idx] * ri[idx % kTB];
   __syncthreads();
   const int lane = tid & 31, w = tid >> 5;
   const int R0 = o + kTB + blockIdx.x * 8 + w * 2, R1 = R0 + 1;
@@ -221,15 +224,12 @@ __global__ void __launch_bounds__(128) k_tchol_trsm(double* S, const double* __r
 #pragma unroll 8
     for (int jl = 0; jl < 32; ++jl) {
       const int j = 32 * hj + jl;
-      const double x0 = __shfl_sync(0xffffffffu, a0[hj], jl) * ri[j];
-      const double x1 = __shfl_sync(0xffffffffu, a1[hj], jl) * ri[j];
+      const double x0 = __shfl_sync(0xffffffffu, a0[hj], jl);
+      const double x1 = __shfl_sync(0xffffffffu, a1[hj], jl);
 #pragma unroll
       for (int h = 0; h < H; ++h) {
         const int mrow = lane + 32 * h;
-        if (mrow == j) {
-          a0[h] = x0;
-          a1[h] = x1;
-        } else if (mrow > j) {
+        if (mrow > j) {
           a0[h] = fma(-x0, Ls[mrow][j], a0[h]);
           a1[h] = fma(-x1, Ls[mrow][j], a1[h]);
         }
@@ -237,8 +237,9 @@ __global__ void __launch_bounds__(128) k_tchol_trsm(double* S, const double* __r
     }
 #pragma unroll
   for (int h = 0; h < H; ++h) {
-    row0[lane + 32 * h] = a0[h];
-    if (has1) row1[lane + 32 * h] = a1[h];
+    const double r = ri[lane + 32 * h];
+    row0[lane + 32 * h] = a0[h] * r;
+    if (has1) row1[lane + 32 * h] = a1[h] * r;
   }
 }
 
