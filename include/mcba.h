@@ -466,8 +466,9 @@ int mcba_batch_solve(mcba_problem* const* problems, int32_t n, int32_t iteration
  * same arithmetic in the same order as mcba_optimize, so every window's
  * trial log, cost and estimates equal its single solve's.  The number of
  * CTAs per window (the cluster size: 4, 8 or 16) is chosen on the first
- * call for a batch by timing each candidate; *cluster_ctas (may be NULL)
- * receives it.  All handles must share the device and the precision, and
+ * call for a batch by timing each candidate, unless *cluster_ctas is 4, 8 or
+ * 16 on entry (then that size is used); NULL or 0 asks for the autotuner,
+ * and *cluster_ctas (when not NULL) receives the size used.  All handles must share the device and the precision, and
  * each window's reduced camera system must have at most 384 unknowns (64
  * free keyframes); MCBA_ERR_INVALID otherwise. */
 int mcba_batch_solve_persistent(mcba_problem* const* problems, int32_t n, int32_t iterations, mcba_stats* stats,

@@ -293,12 +293,14 @@ class LocalBABatch:
         self._arr = arr
         N.check(self.L.mcba_batch_prepare(arr, len(self.solvers)))
 
-    def solve(self, iterations: int = 10, persistent: bool = False):
+    def solve(self, iterations: int = 10, persistent: bool = False, cluster_ctas: int = 0):
+        """cluster_ctas (persistent launch only): 0 lets the autotuner choose
+        the CTAs per window, 4 / 8 / 16 forces that size."""
         n = len(self.solvers)
         stats = (N.Stats * n)()
         ms = ctypes.c_double(0.0)
         if persistent:
-            ctas = ctypes.c_int32(0)
+            ctas = ctypes.c_int32(cluster_ctas)
             N.check(self.L.mcba_batch_solve_persistent(self._arr, n, iterations, stats, ctypes.byref(ms),
                                                        ctypes.byref(ctas)), self.solvers[0].h)
             self.cluster_ctas = ctas.value

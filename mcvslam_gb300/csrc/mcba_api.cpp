@@ -906,7 +906,7 @@ int mcba_batch_solve_persistent(mcba_problem* const* problems, int32_t n, int32_
   }
   std::vector<SolveResult> res(n);
   std::string e;
-  int ctas = 0;
+  int ctas = cluster_ctas ? *cluster_ctas : 0;
   const int r = solver_run_batch_persistent(ss.data(), n, run_options(problems[0], iterations), res.data(), ms_device,
                                             &ctas, &e);
   if (cluster_ctas) *cluster_ctas = ctas;

@@ -211,7 +211,8 @@ int solver_run_batch(Solver* const* ss, int n, const RunOptions& o, SolveResult*
 // windows from a device work queue and each runs a window's whole LM solve
 // (k_windows); the cluster size is chosen by timing the batch on its first
 // call.  Every problem must share the device and the precision, with at
-// most 384 reduced unknowns.  cluster_ctas (may be null): the chosen size.
+// most 384 reduced unknowns.  cluster_ctas (may be null): in, 0 to let the
+// autotuner choose or 4, 8, 16 to use that size; out, the size used.
 int solver_run_batch_persistent(Solver* const* ss, int n, const RunOptions& o, SolveResult* outs, double* ms_device,
                                 int* cluster_ctas, std::string* err);
 // Copies the current device state into hp.

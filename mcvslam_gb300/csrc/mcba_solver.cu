@@ -2365,6 +2365,7 @@ struct PersistentBatch {
   int iters = -1, trials = -1, device = -1, precision = -1;
   double tau = 0.0;
   int C = 0, nclusters = 0;
+  int requested = -1;  // 0: the autotuner chose C; 4, 8, 16: the caller did
   size_t smem = 0;
   std::vector<std::pair<int, float>> tried;  // (CTAs per window, ms) of the autotuner
   DBuf<WinDesc> desc;
@@ -2492,8 +2493,8 @@ int window_clusters(int C, size_t smem) {
 }
 
 template <typename R>
-int run_windows(Solver* const* ss, int n, const RunOptions& o, SolveResult* outs, double* ms_device, int* cluster_ctas,
-                std::string* err) {
+int run_windows(Solver* const* ss, int n, const RunOptions& o, SolveResult* outs, double* ms_device, int request,
+                int* cluster_ctas, std::string* err) {
   Solver* s0 = ss[0];
   cudaStream_t stm = s0->stream;
   std::vector<long long> uids(n);
@@ -2507,7 +2508,7 @@ int run_windows(Solver* const* ss, int n, const RunOptions& o, SolveResult* outs
   PersistentBatch& pb = g_pbatch;
   const bool same = pb.ge && pb.uids == uids && pb.gens == gens && pb.logs == logs && pb.iters == o.iterations &&
                     pb.trials == o.max_trials && pb.tau == o.tau && pb.device == s0->device &&
-                    pb.precision == s0->precision;
+                    pb.precision == s0->precision && pb.requested == request;
   if (!same) {
     pb.release_graph();
     // windows in descending size, so the largest start first
@@ -2520,18 +2521,26 @@ int run_windows(Solver* const* ss, int n, const RunOptions& o, SolveResult* outs
     CK(pb.queue.ensure(1));
     CK(pb.desc.ensure(n));
     // autotuner: CTAs per window (cluster size) by timing the whole batch,
-    // each candidate twice (the first run loads and warms up)
+    // each candidate twice (the first run loads and warms up); a size the
+    // caller asked for is the only candidate and is not timed
     pb.tried.clear();
     int bestC = 0, bestN = 0;
     size_t bestSmem = 0;
     float best = 0.f;
     for (int C : {4, 8, 16}) {
+      if (request && C != request) continue;
       std::vector<WinDesc> d;
       size_t smem = 0;
       if (!window_descs<R>(ss, order, o, C, d, smem, err)) return MCBA_ERR_INVALID;
       const int ncl = window_clusters<R>(C, smem);
       if (ncl < 1) continue;
       const int nclusters = std::min(ncl, n);
+      if (request) {
+        bestC = C;
+        bestN = nclusters;
+        bestSmem = smem;
+        break;
+      }
       CK(cudaMemcpyAsync(pb.desc.p, d.data(), d.size() * sizeof(WinDesc), cudaMemcpyHostToDevice, stm));
       float ms = 0.f;
       for (int rep = 0; rep < 2; ++rep) {
@@ -2577,6 +2586,7 @@ int run_windows(Solver* const* ss, int n, const RunOptions& o, SolveResult* outs
     pb.C = bestC;
     pb.nclusters = bestN;
     pb.smem = bestSmem;
+    pb.requested = request;
   }
   CK(cudaEventRecord(s0->ev[0], stm));
   CK(cudaGraphLaunch(pb.ge, stm));
@@ -2606,6 +2616,11 @@ int run_windows(Solver* const* ss, int n, const RunOptions& o, SolveResult* outs
 int solver_run_batch_persistent(Solver* const* ss, int n, const RunOptions& o, SolveResult* outs, double* ms_device,
                                 int* cluster_ctas, std::string* err) {
   if (n <= 0) return MCBA_OK;
+  const int request = cluster_ctas ? *cluster_ctas : 0;
+  if (request != 0 && request != 4 && request != 8 && request != 16) {
+    if (err) *err = "cluster_ctas must be 0 (autotune), 4, 8 or 16";
+    return MCBA_ERR_INVALID;
+  }
   for (int i = 0; i < n; ++i) {
     if (!ss[i] || !ss[i]->uploaded) {
       if (err) *err = "every problem of the batch must be prepared";
@@ -2620,8 +2635,9 @@ int solver_run_batch_persistent(Solver* const* ss, int n, const RunOptions& o, S
   const int max_log = std::max(1, o.iterations * o.max_trials);
   for (int i = 0; i < n; ++i) CK(ss[i]->log.ensure(max_log));
   std::lock_guard<std::mutex> lk(g_pbatch_mu);
-  return ss[0]->precision == MCBA_PREC_MIXED ? run_windows<float>(ss, n, o, outs, ms_device, cluster_ctas, err)
-                                             : run_windows<double>(ss, n, o, outs, ms_device, cluster_ctas, err);
+  return ss[0]->precision == MCBA_PREC_MIXED
+             ? run_windows<float>(ss, n, o, outs, ms_device, request, cluster_ctas, err)
+             : run_windows<double>(ss, n, o, outs, ms_device, request, cluster_ctas, err);
 }
 
 int solver_run(Solver* s, const RunOptions& o, bool restore, SolveResult& out, std::string* err) {

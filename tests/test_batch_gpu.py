@@ -127,6 +127,36 @@ def test_persistent_window_launch_equals_single_solves(precision, gpu):
             assert abs(a["chi_after"] - r["chi_after"]) <= 1e-9 * abs(r["chi_after"])
 
 
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_persistent_window_launch_at_each_cluster_size(precision, gpu):
+    """The caller may fix the CTAs per window (4, 8 or 16): each size gives
+    the single solves bit for bit (the cluster factorisation applies every
+    tile's updates in one fixed order whatever the number of CTAs); any other
+    size is refused."""
+    from mcvslam_gb300 import _native as N
+
+    wins = _persistent_windows()[::2]
+    iters = 4
+    single = []
+    for pr in wins:
+        with ba.Solver(precision=precision) as s:
+            s.load(pr)
+            st = s.optimize(iters)
+            single.append((st, s.trial_log(), s.state()))
+    with ba.LocalBABatch(wins, precision=precision) as b:
+        for ctas in (16, 4, 8):
+            stats, ms = b.solve(iters, persistent=True, cluster_ctas=ctas)
+            assert b.cluster_ctas == ctas
+            states = b.states()
+            for (st, log, (qt, X)), bst, (bqt, bX), s in zip(single, stats, states, b.solvers):
+                assert bst["final_chi2"] == st["final_chi2"]
+                np.testing.assert_array_equal(s.trial_log(), log)
+                np.testing.assert_array_equal(bqt, qt)
+                np.testing.assert_array_equal(bX, X)
+        with pytest.raises(N.MCBAError):
+            b.solve(iters, persistent=True, cluster_ctas=5)
+
+
 def test_persistent_window_launch_rejects_oversize_windows(gpu):
     """A window whose reduced system exceeds 384 unknowns is refused with
     MCBA_ERR_INVALID (no launch); the graph-branch batch solves it."""
