@@ -1360,8 +1360,10 @@ __device__ void window_solve(const WinArgs& a, const WinDesc& d, int rank, int C
   }
 }
 
-template <typename R>
-__global__ void __launch_bounds__(kWinThreads, 1) k_windows(WinArgs a) {
+// kPerSM: CTAs per SM the launch is compiled for (1, or 2 with at most 96
+// registers a thread and half the shared memory).
+template <typename R, int kPerSM>
+__global__ void __launch_bounds__(kWinThreads, kPerSM) k_windows(WinArgs a) {
   extern __shared__ __align__(16) double dsm[];
   __shared__ WinShared<R> sh;
   __shared__ int s_win;
@@ -2366,6 +2368,7 @@ struct PersistentBatch {
   double tau = 0.0;
   int C = 0, nclusters = 0;
   int requested = -1;  // 0: the autotuner chose C; 4, 8, 16: the caller did
+  int per_sm = 1;      // CTAs per SM the chosen kernel was compiled for
   size_t smem = 0;
   std::vector<std::pair<int, float>> tried;  // (CTAs per window, ms) of the autotuner
   DBuf<WinDesc> desc;
@@ -2385,14 +2388,16 @@ PersistentBatch g_pbatch;
 // Descriptors of the windows (in launch order) for clusters of C CTAs, and
 // the dynamic shared memory the launch needs; false when a window's reduced
 // system does not fit the cluster factorisation.
-template <typename R>
+template <typename R, int P>
 bool window_descs(Solver* const* ss, const std::vector<int>& order, const RunOptions& o, int C,
                   std::vector<WinDesc>& out, size_t& smem, std::string* err) {
-  int dev = 0, max_smem = 0;
+  int dev = 0, max_smem = 0, sm_smem = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  if (P > 1) max_smem = std::min(max_smem, sm_smem / P - 1024);
   cudaFuncAttributes fa{};
-  if (cudaFuncGetAttributes(&fa, k_windows<R>) != cudaSuccess) {
+  if (cudaFuncGetAttributes(&fa, k_windows<R, P>) != cudaSuccess) {
     cudaGetLastError();
     if (err) *err = "k_windows attributes";
     return false;
@@ -2442,7 +2447,7 @@ bool window_descs(Solver* const* ss, const std::vector<int>& order, const RunOpt
   return true;
 }
 
-template <typename R>
+template <typename R, int P>
 cudaError_t launch_windows(const PersistentBatch& pb, int nwin, const RunOptions& o, int C, int nclusters, size_t smem,
                            cudaStream_t st) {
   WinArgs a{pb.desc.p, nwin, pb.queue.p, o.iterations, o.max_trials, o.tau};
@@ -2458,18 +2463,18 @@ cudaError_t launch_windows(const PersistentBatch& pb, int nwin, const RunOptions
   attr.val.clusterDim.z = 1;
   cfg.attrs = &attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, k_windows<R>, a);
+  return cudaLaunchKernelEx(&cfg, k_windows<R, P>, a);
 }
 
 // Clusters of C CTAs that can be resident at once with `smem` bytes each
 // (0 when the configuration cannot launch).
-template <typename R>
+template <typename R, int P>
 int window_clusters(int C, size_t smem) {
   int dev = 0, max_smem = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  if (cudaFuncSetAttribute(k_windows<R>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
-      cudaFuncSetAttribute(k_windows<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+  if (cudaFuncSetAttribute(k_windows<R, P>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
+      cudaFuncSetAttribute(k_windows<R, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
@@ -2485,7 +2490,7 @@ int window_clusters(int C, size_t smem) {
   cfg.attrs = &attr;
   cfg.numAttrs = 1;
   int n = 0;
-  if (cudaOccupancyMaxActiveClusters(&n, k_windows<R>, &cfg) != cudaSuccess) {
+  if (cudaOccupancyMaxActiveClusters(&n, k_windows<R, P>, &cfg) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
@@ -2524,39 +2529,50 @@ int run_windows(Solver* const* ss, int n, const RunOptions& o, SolveResult* outs
     // each candidate twice (the first run loads and warms up); a size the
     // caller asked for is the only candidate and is not timed
     pb.tried.clear();
-    int bestC = 0, bestN = 0;
+    int bestC = 0, bestN = 0, bestP = 1;
     size_t bestSmem = 0;
     float best = 0.f;
-    for (int C : {4, 8, 16}) {
-      if (request && C != request) continue;
-      std::vector<WinDesc> d;
-      size_t smem = 0;
-      if (!window_descs<R>(ss, order, o, C, d, smem, err)) return MCBA_ERR_INVALID;
-      const int ncl = window_clusters<R>(C, smem);
-      if (ncl < 1) continue;
-      const int nclusters = std::min(ncl, n);
-      if (request) {
-        bestC = C;
-        bestN = nclusters;
-        bestSmem = smem;
-        break;
-      }
-      CK(cudaMemcpyAsync(pb.desc.p, d.data(), d.size() * sizeof(WinDesc), cudaMemcpyHostToDevice, stm));
-      float ms = 0.f;
-      for (int rep = 0; rep < 2; ++rep) {
-        CK(cudaMemsetAsync(pb.queue.p, 0, sizeof(int), stm));
-        CK(cudaEventRecord(s0->ev[0], stm));
-        CK(launch_windows<R>(pb, n, o, C, nclusters, smem, stm));
-        CK(cudaEventRecord(s0->ev[1], stm));
-        CK(cudaStreamSynchronize(stm));
-        CK(cudaEventElapsedTime(&ms, s0->ev[0], s0->ev[1]));
-      }
-      pb.tried.emplace_back(C, ms);
-      if (!bestC || ms < best) {
-        best = ms;
-        bestC = C;
-        bestN = nclusters;
-        bestSmem = smem;
+    for (int P : {1, 2}) {
+      if (request && P != 1) continue;
+      for (int C : {4, 8, 16}) {
+        if (request && C != request) continue;
+        std::vector<WinDesc> d;
+        size_t smem = 0;
+        const bool ok = P == 1 ? window_descs<R, 1>(ss, order, o, C, d, smem, err)
+                               : window_descs<R, 2>(ss, order, o, C, d, smem, err);
+        if (!ok) {
+          if (P == 1) return MCBA_ERR_INVALID;
+          continue;  // the half-SM variant may not fit a large window's factorisation
+        }
+        const int ncl = P == 1 ? window_clusters<R, 1>(C, smem) : window_clusters<R, 2>(C, smem);
+        if (ncl < 1) continue;
+        const int nclusters = std::min(ncl, n);
+        if (request) {
+          bestC = C;
+          bestN = nclusters;
+          bestSmem = smem;
+          break;
+        }
+        CK(cudaMemcpyAsync(pb.desc.p, d.data(), d.size() * sizeof(WinDesc), cudaMemcpyHostToDevice, stm));
+        float ms = 0.f;
+        for (int rep = 0; rep < 2; ++rep) {
+          CK(cudaMemsetAsync(pb.queue.p, 0, sizeof(int), stm));
+          CK(cudaEventRecord(s0->ev[0], stm));
+          const cudaError_t le = P == 1 ? launch_windows<R, 1>(pb, n, o, C, nclusters, smem, stm)
+                                        : launch_windows<R, 2>(pb, n, o, C, nclusters, smem, stm);
+          CK(le);
+          CK(cudaEventRecord(s0->ev[1], stm));
+          CK(cudaStreamSynchronize(stm));
+          CK(cudaEventElapsedTime(&ms, s0->ev[0], s0->ev[1]));
+        }
+        pb.tried.emplace_back(C * P, ms);
+        if (!bestC || ms < best) {
+          best = ms;
+          bestC = C;
+          bestN = nclusters;
+          bestSmem = smem;
+          bestP = P;
+        }
       }
     }
     if (!bestC) {
@@ -2565,13 +2581,21 @@ int run_windows(Solver* const* ss, int n, const RunOptions& o, SolveResult* outs
     }
     std::vector<WinDesc> d;
     size_t smem = 0;
-    if (!window_descs<R>(ss, order, o, bestC, d, smem, err)) return MCBA_ERR_INVALID;
+    if (!(bestP == 1 ? window_descs<R, 1>(ss, order, o, bestC, d, smem, err)
+                     : window_descs<R, 2>(ss, order, o, bestC, d, smem, err)))
+      return MCBA_ERR_INVALID;
     CK(cudaMemcpyAsync(pb.desc.p, d.data(), d.size() * sizeof(WinDesc), cudaMemcpyHostToDevice, stm));
-    window_clusters<R>(bestC, smem);
+    if (bestP == 1)
+      window_clusters<R, 1>(bestC, smem);
+    else
+      window_clusters<R, 2>(bestC, smem);
     cudaGraph_t tmp;
     CK(cudaStreamBeginCapture(stm, cudaStreamCaptureModeRelaxed));
     cudaMemsetAsync(pb.queue.p, 0, sizeof(int), stm);
-    launch_windows<R>(pb, n, o, bestC, bestN, bestSmem, stm);
+    if (bestP == 1)
+      launch_windows<R, 1>(pb, n, o, bestC, bestN, bestSmem, stm);
+    else
+      launch_windows<R, 2>(pb, n, o, bestC, bestN, bestSmem, stm);
     CK(cudaStreamEndCapture(stm, &tmp));
     pb.g = tmp;
     CK(cudaGraphInstantiate(&pb.ge, pb.g, 0));
@@ -2584,6 +2608,7 @@ int run_windows(Solver* const* ss, int n, const RunOptions& o, SolveResult* outs
     pb.device = s0->device;
     pb.precision = s0->precision;
     pb.C = bestC;
+    pb.per_sm = bestP;
     pb.nclusters = bestN;
     pb.smem = bestSmem;
     pb.requested = request;
