@@ -1920,15 +1920,12 @@ int capture_leaves(cudaStream_t st, std::vector<cudaGraphNode_t>& leaves, std::s
   return MCBA_OK;
 }
 
-// The whole LM solve as one CUDA graph: prologue, then
-//   while (iterate) { linearise; while (trial) { Schur, Cholesky, update,
-//   cost, decide }; end-of-iteration test }
-// with both loop conditions set on the device (k_lm_decide, k_iter_end).
 // Adds solver s's whole LM solve to graph G as an independent branch: the
 // prologue, then
 //   while (iterate) { linearise; while (trial) { Schur, Cholesky, update,
-//   cost, decide }; end-of-iteration test }
-// with both loop conditions set on the device (k_lm_decide, k_iter_end).
+//   cost and decide }; end-of-iteration test }
+// with both loop conditions set on the device (k_linearize re-arms the
+// trial loop, k_cost_step's last CTA sets it, k_iter_end the outer one).
 template <typename R>
 int add_lm_subgraph(Solver* s, cudaGraph_t G, const RunOptions& o, bool restore, std::string* err) {
   const Launch& L = s->L;
