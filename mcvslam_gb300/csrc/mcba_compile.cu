@@ -54,7 +54,9 @@ constexpr int kRadixBits = 10;
 
 // ------------------------------------------------------------- scan --
 // In place exclusive scan of a[0..n) (the caller's a[n-1] is part of the
-// input; the total is written to a[n]).  One level per 1024 elements.
+// input; the total is written to a[n]).  One level per 1024 elements; a
+// single-block scan writes the total itself, and the add pass of a
+// multi-block scan copies it from the scanned block sums.
 __global__ void __launch_bounds__(256) k_scan_block(int* a, int n, int* sums) {
   __shared__ int warp_tot[8];
   const int base = blockIdx.x * kScanBlock + threadIdx.x * 4;
@@ -80,7 +82,10 @@ __global__ void __launch_bounds__(256) k_scan_block(int* a, int n, int* sums) {
 #pragma unroll
   for (int q = 0; q < 4; ++q)
     if (base + q < n) a[base + q] = excl + loc[q];
-  if (threadIdx.x == 255) sums[blockIdx.x] = wpre + inc;
+  if (threadIdx.x == 255) {
+    sums[blockIdx.x] = wpre + inc;
+    if (gridDim.x == 1) a[n] = wpre + inc;
+  }
 }
 
 __global__ void k_scan_add(int* a, int n, const int* offs) {
@@ -88,10 +93,7 @@ __global__ void k_scan_add(int* a, int n, const int* offs) {
   const int o = offs[blockIdx.x];
   for (int q = 0; q < kScanBlock; q += 256)
     if (i + q < n) a[i + q] += o;
-}
-
-__global__ void k_set_total(int* a, int n, const int* sums) {
-  if (threadIdx.x == 0) a[n] = sums[0];  // single-block scan: its sum is the total
+  if (blockIdx.x == 0 && threadIdx.x == 0) a[n] = offs[gridDim.x];  // the total
 }
 
 __global__ void k_add(int* dst, const int* a, const int* b, int n) {
@@ -519,14 +521,12 @@ class DeviceCompiler {
     int* sums = scan_tmp.p + tmp_off;  // [nb + 1]
     k_scan_block<<<nb, 256, 0, st>>>(a, n, sums);
     if (nb == 1) {
-      k_set_total<<<1, 32, 0, st>>>(a, n, sums);
       CK(cudaGetLastError());
       return MCBA_OK;
     }
     const int r = scan(sums, nb, st, err, tmp_off + nb + 1);
     if (r) return r;
     k_scan_add<<<nb, 256, 0, st>>>(a, n, sums);
-    CK(cudaMemcpyAsync(a + n, sums + nb, sizeof(int), cudaMemcpyDeviceToDevice, st));
     CK(cudaGetLastError());
     return MCBA_OK;
   }

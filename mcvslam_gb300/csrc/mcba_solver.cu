@@ -1415,6 +1415,26 @@ class Solver {
   DBuf<LMState> lm;
   DBuf<mcba_trial_log> log;
   LMState* lm_host = nullptr;
+  // pinned host buffers: the state upload and the read-backs after a solve
+  // go through them as asynchronous copies, one synchronisation each
+  struct Pinned {
+    char* p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t n) {
+      if (n <= cap && p) return cudaSuccess;
+      if (p) cudaFreeHost(p);
+      p = nullptr;
+      cap = 0;
+      const cudaError_t e = cudaMallocHost(&p, std::max<size_t>(n, 256));
+      if (e == cudaSuccess) cap = std::max<size_t>(n, 256);
+      return e;
+    }
+    void release() {
+      if (p) cudaFreeHost(p);
+      p = nullptr;
+      cap = 0;
+    }
+  } h_up, h_rb;
   DeviceCompiler* compiler = nullptr;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   std::vector<cudaEvent_t> evpool;
@@ -1483,6 +1503,8 @@ class Solver {
     lm.release();
     log.release();
     if (lm_host) cudaFreeHost(lm_host);
+    h_up.release();
+    h_rb.release();
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
     for (auto& e : evpool) cudaEventDestroy(e);
@@ -1657,26 +1679,46 @@ int spread_state(Solver* s, bool from_initial, std::string* err) {
 int upload_state(Solver* s, const HostProblem& hp, int U, int64_t& bytes, std::string* err) {
   const int K = (int)hp.poses.size();
   const int P = (int)hp.point_fixed.size();
-  std::vector<double> q(8 * (size_t)std::max(K, 1), 0.0);
+  const int C = (int)hp.cams.size();
+  // one pinned block: poses (8 per pose), points (3 per point, unary
+  // constant points after them), cameras in both precisions
+  const size_t nq = 8 * (size_t)std::max(K, 1), nx = 3 * (size_t)(P + U) + 3;
+  const size_t oq = 0, ox = oq + nq * sizeof(double), ocd = ox + nx * sizeof(double);
+  const size_t ocf = ocd + ((C * sizeof(CamD) + 15) & ~size_t(15)), total = ocf + C * sizeof(CamF);
+  // the previous upload's copies may still read the block
+  CK(cudaStreamSynchronize(s->stream));
+  CK(s->h_up.ensure(total));
+  double* q = reinterpret_cast<double*>(s->h_up.p + oq);
+  double* X = reinterpret_cast<double*>(s->h_up.p + ox);
+  CamD* cd = reinterpret_cast<CamD*>(s->h_up.p + ocd);
+  CamF* cf = reinterpret_cast<CamF*>(s->h_up.p + ocf);
+  std::fill(q, q + nq, 0.0);
   for (int k = 0; k < K; ++k) {
     for (int i = 0; i < 4; ++i) q[8 * k + i] = hp.poses[k].q[i];
     for (int i = 0; i < 3; ++i) q[8 * k + 4 + i] = hp.poses[k].t[i];
   }
-  std::vector<double> X(3 * (size_t)(P + U) + 3, 0.0);
-  std::copy(hp.points.begin(), hp.points.end(), X.begin());
-  std::copy(hp.u_Xw.begin(), hp.u_Xw.begin() + std::min<size_t>(hp.u_Xw.size(), 3 * (size_t)U), X.begin() + 3 * (size_t)P);
-  std::vector<CamD> cd(hp.cams.size());
-  std::vector<CamF> cf(hp.cams.size());
-  for (size_t c = 0; c < hp.cams.size(); ++c) cam_to_dev(hp.cams[c], cd[c], cf[c]);
-  CK(up(s->cd, cd, s->stream, bytes));
-  CK(up(s->cf, cf, s->stream, bytes));
+  std::copy(hp.points.begin(), hp.points.end(), X);
+  const size_t nu = std::min<size_t>(hp.u_Xw.size(), 3 * (size_t)U);
+  std::copy(hp.u_Xw.begin(), hp.u_Xw.begin() + nu, X + 3 * (size_t)P);
+  std::fill(X + 3 * (size_t)P + nu, X + nx, 0.0);
+  for (int c = 0; c < C; ++c) cam_to_dev(hp.cams[c], cd[c], cf[c]);
+  auto put = [&](void* dst, const void* src, size_t n) -> cudaError_t {
+    bytes += (int64_t)n;
+    return n ? cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, s->stream) : cudaSuccess;
+  };
+  CK(s->cd.ensure(std::max(C, 1)));
+  CK(s->cf.ensure(std::max(C, 1)));
+  CK(s->pose_qt[0].ensure(nq));
+  CK(s->Xd[0].ensure(nx));
+  CK(put(s->cd.p, cd, C * sizeof(CamD)));
+  CK(put(s->cf.p, cf, C * sizeof(CamF)));
+  CK(put(s->pose_qt[0].p, q, nq * sizeof(double)));
+  CK(put(s->Xd[0].p, X, nx * sizeof(double)));
   const int NP = P + U;
-  CK(up(s->pose_qt[0], q, s->stream, bytes));
-  CK(up(s->Xd[0], X, s->stream, bytes));
-  CK(s->pose_qt[1].ensure(q.size()));
-  CK(s->Xd[1].ensure(X.size()));
-  CK(s->pose_qt0.ensure(q.size()));
-  CK(s->Xd0.ensure(X.size()));
+  CK(s->pose_qt[1].ensure(nq));
+  CK(s->Xd[1].ensure(nx));
+  CK(s->pose_qt0.ensure(nq));
+  CK(s->Xd0.ensure(nx));
   for (int b = 0; b < 2; ++b) {
     CK(s->pd[b].ensure(std::max(K, 1)));
     CK(s->pf[b].ensure(std::max(K, 1)));
@@ -2018,15 +2060,19 @@ int finish_run(Solver* s, const RunOptions& o, SolveResult& out, std::string* er
   out.trials = s->lm_host->total_trials;
   const int nl = std::min(s->lm_host->n_log, max_log);
   out.log.resize(nl);
-  if (nl) {
-    CK(cudaMemcpy(out.log.data(), s->log.p, nl * sizeof(mcba_trial_log), cudaMemcpyDeviceToHost));
-    out.d2h += nl * sizeof(mcba_trial_log);
-  }
-  // Hpp of the last linearisation (DumpCalculationGraph)
-  if (L.Kf && out.iterations > 0) {
-    out.hpp.resize((size_t)L.Kf * 36);
-    CK(cudaMemcpy(out.hpp.data(), s->Hpp.p, out.hpp.size() * sizeof(double), cudaMemcpyDeviceToHost));
-    out.d2h += out.hpp.size() * sizeof(double);
+  // the trial log and the Hpp of the last linearisation (DumpCalculationGraph)
+  // through the pinned read-back buffer, one synchronisation
+  const size_t nh = (L.Kf && out.iterations > 0) ? (size_t)L.Kf * 36 : 0;
+  const size_t blog = nl * sizeof(mcba_trial_log), bh = nh * sizeof(double);
+  out.hpp.resize(nh);
+  if (blog + bh) {
+    CK(s->h_rb.ensure(blog + bh));
+    if (blog) CK(cudaMemcpyAsync(s->h_rb.p, s->log.p, blog, cudaMemcpyDeviceToHost, s->stream));
+    if (bh) CK(cudaMemcpyAsync(s->h_rb.p + blog, s->Hpp.p, bh, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    if (blog) std::memcpy(out.log.data(), s->h_rb.p, blog);
+    if (bh) std::memcpy(out.hpp.data(), s->h_rb.p + blog, bh);
+    out.d2h += (int64_t)(blog + bh);
   }
   return MCBA_OK;
 }
@@ -2683,15 +2729,15 @@ int solver_download(Solver* s, HostProblem& hp, SolveResult& out, std::string* e
   CK(cudaSetDevice(s->device));
   const int K = (int)hp.poses.size(), P = (int)hp.point_fixed.size();
   const int cur = s->lm_host->cur;
-  std::vector<double> q(8 * (size_t)std::max(K, 1));
-  if (K) {
-    CK(cudaMemcpy(q.data(), s->pose_qt[cur].p, 8 * (size_t)K * sizeof(double), cudaMemcpyDeviceToHost));
-    out.d2h += 8 * (int64_t)K * sizeof(double);
-  }
-  if (P) {
-    CK(cudaMemcpy(hp.points.data(), s->Xd[cur].p, 3 * (size_t)P * sizeof(double), cudaMemcpyDeviceToHost));
-    out.d2h += 3 * (int64_t)P * sizeof(double);
-  }
+  const size_t bq = 8 * (size_t)K * sizeof(double), bx = 3 * (size_t)P * sizeof(double);
+  if (!(bq + bx)) return MCBA_OK;
+  CK(s->h_rb.ensure(bq + bx));
+  if (K) CK(cudaMemcpyAsync(s->h_rb.p, s->pose_qt[cur].p, bq, cudaMemcpyDeviceToHost, s->stream));
+  if (P) CK(cudaMemcpyAsync(s->h_rb.p + bq, s->Xd[cur].p, bx, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  out.d2h += (int64_t)(bq + bx);
+  if (P) std::memcpy(hp.points.data(), s->h_rb.p + bq, bx);
+  const double* q = reinterpret_cast<const double*>(s->h_rb.p);
   for (int k = 0; k < K; ++k) {
     for (int i = 0; i < 4; ++i) hp.poses[k].q[i] = q[8 * k + i];
     for (int i = 0; i < 3; ++i) hp.poses[k].t[i] = q[8 * k + 4 + i];
