@@ -57,14 +57,17 @@ class TrialLog(ctypes.Structure):
 
 
 class ProblemDesc(ctypes.Structure):
+    """mcba_problem_desc; pointer fields as plain host addresses (an address
+    is assigned a quarter as fast as a typed ctypes pointer is built)."""
     _fields_ = [
-        ("n_cams", ctypes.c_int32), ("cam_K", c_float_p), ("cam_bf", c_float_p), ("cam_Tcb", c_float_p),
-        ("n_poses", ctypes.c_int32), ("pose_Tcw", c_float_p), ("pose_fixed", c_u8_p),
-        ("n_points", ctypes.c_int32), ("point_Xw", c_float_p), ("point_fixed", c_u8_p),
-        ("n_edges", ctypes.c_int32), ("edge_type", c_u8_p), ("edge_pose", c_i32_p),
-        ("edge_point", c_i32_p), ("edge_cam", c_i32_p), ("edge_obs", c_float_p),
-        ("edge_info", c_float_p), ("edge_delta", c_float_p), ("edge_robust", c_u8_p),
-        ("edge_level", c_u8_p),
+        ("n_cams", ctypes.c_int32), ("cam_K", ctypes.c_void_p), ("cam_bf", ctypes.c_void_p),
+        ("cam_Tcb", ctypes.c_void_p),
+        ("n_poses", ctypes.c_int32), ("pose_Tcw", ctypes.c_void_p), ("pose_fixed", ctypes.c_void_p),
+        ("n_points", ctypes.c_int32), ("point_Xw", ctypes.c_void_p), ("point_fixed", ctypes.c_void_p),
+        ("n_edges", ctypes.c_int32), ("edge_type", ctypes.c_void_p), ("edge_pose", ctypes.c_void_p),
+        ("edge_point", ctypes.c_void_p), ("edge_cam", ctypes.c_void_p), ("edge_obs", ctypes.c_void_p),
+        ("edge_info", ctypes.c_void_p), ("edge_delta", ctypes.c_void_p), ("edge_robust", ctypes.c_void_p),
+        ("edge_level", ctypes.c_void_p),
     ]
 
 

@@ -72,35 +72,23 @@ class Solver:
         self.close()
 
     # -- graph
+    _LOAD_ARRAYS = (("cam_K", np.float32), ("cam_bf", np.float32), ("cam_Tcb", np.float32),
+                    ("pose_Tcw", np.float32), ("pose_fixed", np.uint8), ("point_Xw", np.float32),
+                    ("point_fixed", np.uint8), ("edge_type", np.uint8), ("edge_pose", np.int32),
+                    ("edge_point", np.int32), ("edge_cam", np.int32), ("edge_obs", np.float32),
+                    ("edge_info", np.float32), ("edge_delta", np.float32), ("edge_robust", np.uint8),
+                    ("edge_level", np.uint8))
+
     def load(self, pr: synth.Problem) -> "Solver":
-        keep = {}
-
-        def arr(name, dt):
-            a = np.ascontiguousarray(getattr(pr, name), dtype=dt)
-            keep[name] = a
-            return a
-
         d = N.ProblemDesc()
-        d.n_cams = pr.n_cams
-        d.cam_K = _p(arr("cam_K", np.float32), N.c_float_p)
-        d.cam_bf = _p(arr("cam_bf", np.float32), N.c_float_p)
-        d.cam_Tcb = _p(arr("cam_Tcb", np.float32), N.c_float_p)
-        d.n_poses = pr.n_poses
-        d.pose_Tcw = _p(arr("pose_Tcw", np.float32), N.c_float_p)
-        d.pose_fixed = _p(arr("pose_fixed", np.uint8), N.c_u8_p)
-        d.n_points = pr.n_points
-        d.point_Xw = _p(arr("point_Xw", np.float32), N.c_float_p)
-        d.point_fixed = _p(arr("point_fixed", np.uint8), N.c_u8_p)
-        d.n_edges = pr.n_edges
-        d.edge_type = _p(arr("edge_type", np.uint8), N.c_u8_p)
-        d.edge_pose = _p(arr("edge_pose", np.int32), N.c_i32_p)
-        d.edge_point = _p(arr("edge_point", np.int32), N.c_i32_p)
-        d.edge_cam = _p(arr("edge_cam", np.int32), N.c_i32_p)
-        d.edge_obs = _p(arr("edge_obs", np.float32), N.c_float_p)
-        d.edge_info = _p(arr("edge_info", np.float32), N.c_float_p)
-        d.edge_delta = _p(arr("edge_delta", np.float32), N.c_float_p)
-        d.edge_robust = _p(arr("edge_robust", np.uint8), N.c_u8_p)
-        d.edge_level = _p(arr("edge_level", np.uint8), N.c_u8_p)
+        d.n_cams, d.n_poses, d.n_points, d.n_edges = pr.n_cams, pr.n_poses, pr.n_points, pr.n_edges
+        keep = []  # converted copies live until mcba_load has copied them
+        for name, dt in self._LOAD_ARRAYS:
+            a = getattr(pr, name)
+            if a.dtype != dt or not a.flags["C_CONTIGUOUS"]:
+                a = np.ascontiguousarray(a, dtype=dt)
+            keep.append(a)
+            setattr(d, name, a.ctypes.data if a.size else None)
         N.check(self.L.mcba_load(self.h, ctypes.byref(d)), self.h)
         self.n_poses, self.n_points, self.n_edges = pr.n_poses, pr.n_points, pr.n_edges
         return self

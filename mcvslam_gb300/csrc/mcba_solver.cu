@@ -332,16 +332,56 @@ __device__ __forceinline__ void pose_lin_one(const double* q, PoseLinD* pd, Pose
   *pf = f;
 }
 
-__global__ void k_pose_lin(const double* __restrict__ qt, int n, PoseLinD* pd, PoseLinF* pf) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  pose_lin_one(qt + 8 * (size_t)i, pd + i, pf + i);
-}
+// Both halves of the double-buffered state, with their rotation matrices
+// and float copies, from one source (the uploaded state or the saved
+// initial one), in one launch; keep_q / keep_x (may be null) also receive
+// the source, as the saved initial state.
+struct SpreadArgs {
+  const double* src_q;
+  const double* src_x;
+  int K, NP;
+  double* q[2];
+  double* x[2];
+  PoseLinD* pd[2];
+  PoseLinF* pf[2];
+  float4* xf[2];
+  double* keep_q;
+  double* keep_x;
+};
 
-__global__ void k_points_f(const double* __restrict__ X, int n, float4* Xf) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  Xf[i] = make_float4((float)X[3 * (size_t)i], (float)X[3 * (size_t)i + 1], (float)X[3 * (size_t)i + 2], 0.f);
+__global__ void k_spread(SpreadArgs a) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.K + a.NP; i += gridDim.x * blockDim.x) {
+    if (i < a.K) {
+      double q[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) q[k] = a.src_q[8 * (size_t)i + k];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        a.q[0][8 * (size_t)i + k] = q[k];
+        a.q[1][8 * (size_t)i + k] = q[k];
+        if (a.keep_q) a.keep_q[8 * (size_t)i + k] = q[k];
+      }
+      pose_lin_one(q, a.pd[0] + i, a.pf[0] + i);
+      a.pd[1][i] = a.pd[0][i];
+      a.pf[1][i] = a.pf[0][i];
+    } else {
+      const size_t j = (size_t)(i - a.K);
+      const double x0 = a.src_x[3 * j], x1 = a.src_x[3 * j + 1], x2 = a.src_x[3 * j + 2];
+      const float4 f = make_float4((float)x0, (float)x1, (float)x2, 0.f);
+#pragma unroll
+      for (int b = 0; b < 2; ++b) {
+        a.x[b][3 * j] = x0;
+        a.x[b][3 * j + 1] = x1;
+        a.x[b][3 * j + 2] = x2;
+        a.xf[b][j] = f;
+      }
+      if (a.keep_x) {
+        a.keep_x[3 * j] = x0;
+        a.keep_x[3 * j + 1] = x1;
+        a.keep_x[3 * j + 2] = x2;
+      }
+    }
+  }
 }
 
 // Per-edge linearisation (buildSystem's edge loop, block_solver.hpp:490-506).
@@ -1653,25 +1693,28 @@ void cam_to_dev(const HostCamera& c, CamD& d, CamF& f) {
 
 // Both halves of the double-buffered state from the buffer-0 copy (or from
 // the saved initial state), with the derived rotation matrices / float copies.
+// Both halves of the state from the saved initial state (from_initial) or
+// from half 0 just uploaded, which is then also saved as the initial state.
 int spread_state(Solver* s, bool from_initial, std::string* err) {
   const Launch& L = s->L;
-  cudaStream_t st = s->stream;
+  if (L.K + L.NP == 0) return MCBA_OK;
+  SpreadArgs a{};
+  a.src_q = from_initial ? s->pose_qt0.p : s->pose_qt[0].p;
+  a.src_x = from_initial ? s->Xd0.p : s->Xd[0].p;
+  a.K = L.K;
+  a.NP = L.NP;
   for (int b = 0; b < 2; ++b) {
-    const double* srcq = from_initial ? s->pose_qt0.p : s->pose_qt[0].p;
-    const double* srcx = from_initial ? s->Xd0.p : s->Xd[0].p;
-    if (from_initial || b == 1) {
-      if (L.K) CK(cudaMemcpyAsync(s->pose_qt[b].p, srcq, 8 * (size_t)L.K * sizeof(double), cudaMemcpyDeviceToDevice, st));
-      if (L.NP) CK(cudaMemcpyAsync(s->Xd[b].p, srcx, 3 * (size_t)L.NP * sizeof(double), cudaMemcpyDeviceToDevice, st));
-    }
-    if (L.K) {
-      k_pose_lin<<<(L.K + 127) / 128, 128, 0, st>>>(s->pose_qt[b].p, L.K, s->pd[b].p, s->pf[b].p);
-      s->launches++;
-    }
-    if (L.NP) {
-      k_points_f<<<(L.NP + 255) / 256, 256, 0, st>>>(s->Xd[b].p, L.NP, s->Xf[b].p);
-      s->launches++;
-    }
+    a.q[b] = s->pose_qt[b].p;
+    a.x[b] = s->Xd[b].p;
+    a.pd[b] = s->pd[b].p;
+    a.pf[b] = s->pf[b].p;
+    a.xf[b] = s->Xf[b].p;
   }
+  a.keep_q = from_initial ? nullptr : s->pose_qt0.p;
+  a.keep_x = from_initial ? nullptr : s->Xd0.p;
+  const int n = L.K + L.NP;
+  k_spread<<<std::min((n + 255) / 256, 1216), 256, 0, s->stream>>>(a);
+  s->launches++;
   CK(cudaGetLastError());
   return MCBA_OK;
 }
@@ -1727,8 +1770,6 @@ int upload_state(Solver* s, const HostProblem& hp, int U, int64_t& bytes, std::s
   s->L.K = K;
   s->L.P = P;
   s->L.NP = NP;
-  if (K) CK(cudaMemcpyAsync(s->pose_qt0.p, s->pose_qt[0].p, 8 * (size_t)K * sizeof(double), cudaMemcpyDeviceToDevice, s->stream));
-  if (NP) CK(cudaMemcpyAsync(s->Xd0.p, s->Xd[0].p, 3 * (size_t)NP * sizeof(double), cudaMemcpyDeviceToDevice, s->stream));
   return spread_state(s, false, err);
 }
 
