@@ -643,31 +643,46 @@ int mcba_load(mcba_problem* p, const mcba_problem_desc* d) {
   // contiguous edge ranges in parallel (the failing edge is looked up only
   // when a range reports a problem)
   HostPool& pool = HostPool::get();
-  pool.run(9, [&](int task) {
+  // the arrays are sized first (the bulk ones without a zero fill), then
+  // filled in pieces of at most 32K edges spread over the pool, so that no
+  // single array (the 12-byte observations) is one thread's work
+  h.e_type.resize(E);
+  h.e_pose.resize(E);
+  h.e_point.resize(E);
+  h.e_cam.resize(E);
+  h.e_obs.resize(3 * E);
+  h.e_info.resize(E);
+  h.e_delta.resize(E);
+  h.e_robust.resize(E);
+  h.e_level.resize(E);
+  constexpr size_t kPieceEdges = 32768;
+  const int npieces = (int)((E + kPieceEdges - 1) / kPieceEdges);
+  pool.run(npieces * 9, [&](int t) {
+    const int task = t % 9;
+    const size_t b = (size_t)(t / 9) * kPieceEdges, e = std::min(E, b + kPieceEdges), n = e - b;
     switch (task) {
-      case 0: h.e_type.assign(d->edge_type, d->edge_type + E); break;
-      case 1: h.e_pose.assign(d->edge_pose, d->edge_pose + E); break;
-      case 2: h.e_point.assign(d->edge_point, d->edge_point + E); break;
-      case 3: h.e_cam.assign(d->edge_cam, d->edge_cam + E); break;
-      case 4: h.e_obs.assign(d->edge_obs, d->edge_obs + 3 * E); break;
+      case 0: std::memcpy(h.e_type.data() + b, d->edge_type + b, n); break;
+      case 1: std::memcpy(h.e_pose.data() + b, d->edge_pose + b, n * sizeof(int32_t)); break;
+      case 2: std::memcpy(h.e_point.data() + b, d->edge_point + b, n * sizeof(int32_t)); break;
+      case 3: std::memcpy(h.e_cam.data() + b, d->edge_cam + b, n * sizeof(int32_t)); break;
+      case 4: std::memcpy(h.e_obs.data() + 3 * b, d->edge_obs + 3 * b, 3 * n * sizeof(float)); break;
       case 5:
-        if (d->edge_info) h.e_info.assign(d->edge_info, d->edge_info + E);
-        else h.e_info.assign(E, 1.f);
+        if (d->edge_info) std::memcpy(h.e_info.data() + b, d->edge_info + b, n * sizeof(float));
+        else std::fill(h.e_info.begin() + b, h.e_info.begin() + e, 1.f);
         break;
       case 6:
-        if (d->edge_delta) h.e_delta.assign(d->edge_delta, d->edge_delta + E);
-        else h.e_delta.assign(E, 0.f);
+        if (d->edge_delta) std::memcpy(h.e_delta.data() + b, d->edge_delta + b, n * sizeof(float));
+        else std::fill(h.e_delta.begin() + b, h.e_delta.begin() + e, 0.f);
         break;
       case 7:
-        h.e_robust.resize(E);
         if (d->edge_robust)
-          for (size_t i = 0; i < E; ++i) h.e_robust[i] = d->edge_robust[i] ? 1 : 0;
+          for (size_t i = b; i < e; ++i) h.e_robust[i] = d->edge_robust[i] ? 1 : 0;
         else
-          std::fill(h.e_robust.begin(), h.e_robust.end(), (uint8_t)1);
+          std::fill(h.e_robust.begin() + b, h.e_robust.begin() + e, (uint8_t)1);
         break;
       default:
-        if (d->edge_level) h.e_level.assign(d->edge_level, d->edge_level + E);
-        else h.e_level.assign(E, 0);
+        if (d->edge_level) std::memcpy(h.e_level.data() + b, d->edge_level + b, n);
+        else std::fill(h.e_level.begin() + b, h.e_level.begin() + e, (uint8_t)0);
         break;
     }
   });

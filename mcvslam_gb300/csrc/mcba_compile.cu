@@ -474,11 +474,18 @@ inline int blocks(int n, int t = 256) { return std::max(1, (n + t - 1) / t); }
 
 }  // namespace
 
+// One staging-copy task: bytes [b, e) of raw array a.
+struct Piece {
+  int a;
+  size_t b, e;
+};
+
 class DeviceCompiler {
  public:
   char* h_stage = nullptr;  // pinned staging of the raw graph
   size_t h_cap = 0;
   int* h_sizes = nullptr;   // pinned
+  std::vector<Piece> pieces;  // staging copy tasks (kept for their capacity)
   DBuf<char> d_raw;
   Raw raw{};
   int Eall = 0, K = 0, P = 0, U = 0, Kf = 0, Lf = 0, E = 0, Ec = 0, nchunk = 0, npairs = 0, nblk = 0, npc = 0;
@@ -582,25 +589,27 @@ int compiler_phase1(DeviceCompiler* c, const HostProblem& hp, cudaStream_t st, S
   }
   if (!c->h_sizes) CK(cudaMallocHost(&c->h_sizes, 16 * sizeof(int)));
   char* h = c->h_stage;
-  // the staging copies, one array per host-pool task
-  HostPool::get().run(11, [&](int a) {
-    if (a < 9 && !Eall) return;
-    switch (a) {
-      case 0: std::memcpy(h + off[0], hp.e_pose.data(), sizes[0]); break;
-      case 1: std::memcpy(h + off[1], hp.e_point.data(), sizes[1]); break;
-      case 2: std::memcpy(h + off[2], hp.e_type.data(), sizes[2]); break;
-      case 3: {
-        uint8_t* cam8 = reinterpret_cast<uint8_t*>(h + off[3]);
-        for (int i = 0; i < Eall; ++i) cam8[i] = (uint8_t)hp.e_cam[i];
-        break;
-      }
-      case 4: std::memcpy(h + off[4], hp.e_level.data(), sizes[4]); break;
-      case 5: std::memcpy(h + off[5], hp.e_robust.data(), sizes[5]); break;
-      case 6: std::memcpy(h + off[6], hp.e_info.data(), sizes[6]); break;
-      case 7: std::memcpy(h + off[7], hp.e_delta.data(), sizes[7]); break;
-      case 8: std::memcpy(h + off[8], hp.e_obs.data(), sizes[8]); break;
-      case 9: if (K) std::memcpy(h + off[9], hp.pose_fixed.data(), sizes[9]); break;
-      default: if (P) std::memcpy(h + off[10], hp.point_fixed.data(), sizes[10]); break;
+  // the staging copies in pieces of at most 128 KB spread over the host
+  // pool (one array per task left the 12-byte observations on one thread,
+  // the longest task by far); the camera indices are narrowed to bytes
+  const void* src[11] = {hp.e_pose.data(),  hp.e_point.data(), hp.e_type.data(),  nullptr,
+                         hp.e_level.data(), hp.e_robust.data(), hp.e_info.data(), hp.e_delta.data(),
+                         hp.e_obs.data(),   hp.pose_fixed.data(), hp.point_fixed.data()};
+  constexpr size_t kPiece = 128 * 1024;
+  std::vector<Piece>& pieces = c->pieces;
+  pieces.clear();
+  for (int a = 0; a < 11; ++a) {
+    if (a < 9 && !Eall) continue;
+    const size_t n = sizes[a];  // bytes (for the camera indices: bytes of the output)
+    for (size_t b = 0; b < n; b += kPiece) pieces.push_back(Piece{a, b, std::min(n, b + kPiece)});
+  }
+  HostPool::get().run((int)pieces.size(), [&](int t) {
+    const Piece& q = pieces[t];
+    if (q.a == 3) {
+      uint8_t* cam8 = reinterpret_cast<uint8_t*>(h + off[3]);
+      for (size_t i = q.b; i < q.e; ++i) cam8[i] = (uint8_t)hp.e_cam[i];
+    } else {
+      std::memcpy(h + off[q.a] + q.b, static_cast<const char*>(src[q.a]) + q.b, q.e - q.b);
     }
   });
   CK(c->d_raw.ensure(cur));

@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "mcba.h"
@@ -26,6 +27,30 @@ struct HostCamera {
   QT T_cb;     // T_cam_body
 };
 
+// std::allocator whose value-initialisation leaves elements uninitialised,
+// so resize() on the bulk arrays costs no zero fill (the bulk load writes
+// every element right after).
+template <typename T>
+struct NoInitAlloc : std::allocator<T> {
+  template <typename U>
+  struct rebind {
+    using other = NoInitAlloc<U>;
+  };
+  NoInitAlloc() = default;
+  template <typename U>
+  NoInitAlloc(const NoInitAlloc<U>&) {}
+  template <typename U>
+  void construct(U* p) noexcept {
+    ::new (static_cast<void*>(p)) U;
+  }
+  template <typename U, typename... A>
+  void construct(U* p, A&&... a) {
+    ::new (static_cast<void*>(p)) U(std::forward<A>(a)...);
+  }
+};
+template <typename T>
+using BulkVec = std::vector<T, NoInitAlloc<T>>;
+
 // The graph as the caller built it (vertex and edge ids = insertion order).
 struct HostProblem {
   std::vector<HostCamera> cams;
@@ -34,9 +59,9 @@ struct HostProblem {
   std::vector<double> points;  // [P][3]
   std::vector<uint8_t> point_fixed;
   std::vector<uint8_t> e_type;
-  std::vector<int32_t> e_pose, e_point, e_cam;
-  std::vector<float> e_obs;  // [E][3]
-  std::vector<float> e_info, e_delta;
+  BulkVec<int32_t> e_pose, e_point, e_cam;
+  BulkVec<float> e_obs;  // [E][3]
+  BulkVec<float> e_info, e_delta;
   std::vector<uint8_t> e_robust, e_level;
   std::vector<double> u_Xw;  // [U][3] constant points of the unary edges, in edge order
 
