@@ -569,7 +569,13 @@ __device__ void chain_cta(const Geo& g, const double* S, double* ws, double* x, 
   //      Right-hand-side panel J is done only after every L_JI was (its
   //      updates read them), and the last right-hand-side tile waited above
   //      covers row nblk-1; so warp 8 waits for the right-hand-side panels
-  //      and the inverses, one lane per row, then issues rows.
+  //      and the inverses, one lane per row, then issues rows.  Issuing a
+  //      row's copies takes ~0.45 us (one bulk copy per tile), so with four
+  //      or more slots only the first two rows are issued here and row J-2
+  //      in iteration J, two iterations ahead of its use and into the slot
+  //      of a row already done; with three slots, the first three here and
+  //      row J+2-R in iteration J.
+  const int ahead = R >= 4 ? 2 : R;
   if (warp == 8) {
     if (lane < nblk - 1) {
       wait_ge(flag_at(fl, nblk, nblk, lane), lane + 1, abort_word);
@@ -577,7 +583,8 @@ __device__ void chain_cta(const Geo& g, const double* S, double* ws, double* x, 
     }
     __syncwarp();
     fence_proxy_async();
-    for (int J = nblk - 1; J >= 0 && J >= nblk - R; --J) issue_row(g, ws, slot(J), bars + J % R, J, J < nblk - 1);
+    for (int J = nblk - 1; J >= 0 && J >= nblk - ahead; --J)
+      issue_row(g, ws, slot(J), bars + J % R, J, J < nblk - 1);
   }
   __syncthreads();
   for (int e = tid; e < kB * (nblk - 1); e += kThreads) t[e] = __ldcg(ws + g.rhs_y() + e);
@@ -636,8 +643,11 @@ __device__ void chain_cta(const Geo& g, const double* S, double* ws, double* x, 
         }
       }
     } else if (warp == 8) {
-      const int Jn = J + 2 - R;
-      if (Jn >= 0 && Jn < nblk - R) issue_row(g, ws, slot(Jn), bars + Jn % R, Jn, true);
+      const int Jn = R >= 4 ? J - 2 : J + 2 - R;
+      if (Jn >= 0 && Jn < nblk - ahead) {
+        fence_proxy_async();  // the slot's earlier reads come before the copies into it
+        issue_row(g, ws, slot(Jn), bars + Jn % R, Jn, true);
+      }
     }
     __syncthreads();
   }
