@@ -24,12 +24,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_ldlt_cluster(const double* S, d
 
 }  // namespace
 
+size_t chol_cluster_ws_doubles(int ld, int n) {
+  return std::max((size_t)(ld + 32) * ld, make_geo(16, ld, n, 1).ws_doubles());
+}
+
 int chol_cluster_plan(int ld, int n, CholPlan* plan) {
   plan->ok = false;
   const int nblk = (n + kB - 1) / kB;
   if (n <= 0 || ld < kB * nblk || nblk > kMaxBlk) return 0;
-  // the tiles, flags and inverses must fit the (ld + 32) x ld workspace
-  if (make_geo(16, ld, n, 1).ws_doubles() > (size_t)(ld + 32) * ld) return 0;
   int dev = 0;
   cudaGetDevice(&dev);
   int max_smem = 0;

@@ -53,9 +53,11 @@
 //     whichever die the flag's line maps to, and the factorisation time
 //     depended on that (98 or 104 us at n = 168 on GB300, by the page).
 //   * Backward solve L^T x = y on the chain CTA, block row by block row:
-//     rows of L and M arrive in shared memory by bulk asynchronous copies
-//     (one per tile), and per block row only two 16x16 products lie on the
-//     dependency chain (u = t_J - L_{J+1,J}^T x_{J+1}, x_J = M_J u).
+//     rows of L, M and P arrive in shared memory by bulk asynchronous copies
+//     (one per tile), and per block row only one 16x16 product lies on the
+//     dependency chain (x_J = M_J t_J - P_J x_{J+1}, with P_J =
+//     M_J L_{J+1,J}^T formed beside M_J by the lookahead worker and M_J t_J
+//     by a second warp).
 //
 // Every wait has a time limit (%globaltimer); a wait that runs out sets an
 // abort word, and the solve then reports failure (*solve_ok = 0) instead of
@@ -106,6 +108,7 @@ constexpr int kBarOutFull = 4;  // workers: result buffer b ready for warp 8, id
 constexpr int kBarOutFree = 6;  // workers: result buffer b stored, ids 6, 7
 constexpr int kBarInFull = 8;   // workers: inputs of the next task staged by warp 9, ids 8, 9
 constexpr int kBarInFree = 10;  // workers: stage b read by warps 0-7, ids 10, 11
+constexpr int kBarBack = 12;    // chain CTA, backward solve: warp 9's M_J t_J ready for warp 0
 
 // Reciprocal of a pivot: rcp.approx.ftz.f64 (relative error ~1e-6), then one
 // cubic Newton-Raphson step y (1 + e + e^2), e = 1 - d y, which leaves an
@@ -278,13 +281,15 @@ struct Geo {
                           // bounded waits sets it so that a wait runs out)
   // workspace (doubles): nblk x nblk tiles of 256, then the right-hand-side
   // rows W, 1/d and y (16 nblk each), then the inverses M_J (256 each,
+  // transposed), then the products P_J = M_J L_{J+1,J}^T (256 each,
   // transposed), each part 256-byte aligned
   __host__ __device__ size_t tile_off(int i, int j) const { return ((size_t)i * nblk + j) * kTile; }
   __host__ __device__ size_t rhs_w() const { return (size_t)nblk * nblk * kTile; }
   __host__ __device__ size_t rhs_rd() const { return rhs_w() + (size_t)kB * nblk; }
   __host__ __device__ size_t rhs_y() const { return rhs_rd() + (size_t)kB * nblk; }
   __host__ __device__ size_t m_offset() const { return ((rhs_y() + (size_t)kB * nblk + 31) / 32) * 32; }
-  __host__ __device__ size_t ws_doubles() const { return m_offset() + (size_t)nblk * kTile; }
+  __host__ __device__ size_t p_offset() const { return m_offset() + (size_t)nblk * kTile; }
+  __host__ __device__ size_t ws_doubles() const { return p_offset() + (size_t)nblk * kTile; }
   // version flags (ints, in the chain CTA's shared memory): one per tile
   // ((nblk + 1) x nblk, right-hand-side row last), one per inverse M_J, and
   // the abort word
@@ -303,7 +308,9 @@ struct Geo {
   __host__ __device__ size_t c_lk() const { return c_lp() + kPadTile; }
   __host__ __device__ size_t c_rx(int b) const { return c_lk() + kPadTile + kB + b; }
   __host__ __device__ size_t c_end() const { return c_rx(2); }
-  // backward solve, after that: t, x, the slot mbarriers, R row slots
+  // backward solve, after that: t, x, the slot mbarriers, R row slots of
+  // nblk tiles (row J: L_JI at positions I < J, M_J at J, P_J at J+1; the
+  // last row has no P)
   __host__ __device__ size_t b_t() const { return c_end(); }
   __host__ __device__ size_t b_x() const { return b_t() + (size_t)kB * nblk; }
   __host__ __device__ size_t b_bar() const { return b_x() + (size_t)kB * nblk; }
@@ -401,16 +408,19 @@ __device__ void diag_ldlt(double* T, double* rd, double* sq, int* solve_ok) {
 }
 
 // One backward-solve row J into a shared-memory slot by bulk asynchronous
-// copies, one per tile: L_JI (I < J) into positions I, M_J into position J
-// (unless the chain CTA computed it in place).  Run by one whole warp once
-// every producer is known to be done.
+// copies, one per tile: L_JI (I < J) into positions I, and, unless the chain
+// CTA computed M_J in place (the last row), M_J into position J and P_J into
+// position J+1.  Run by one whole warp once every producer is known to be
+// done.
 __device__ void issue_row(const Geo& g, const double* ws, double* slot, uint64_t* bar, int J, bool with_m) {
   const int lane = threadIdx.x & 31;
-  const int ncopy = J + (with_m ? 1 : 0);
+  const int ncopy = J + (with_m ? 2 : 0);
   if (lane == 0) mbar_expect_tx(bar, (unsigned)ncopy * kTile * sizeof(double));
   __syncwarp();
   for (int I = lane; I < ncopy; I += 32) {
-    const double* src = (I < J) ? ws + g.tile_off(I, J) : ws + g.m_offset() + (size_t)J * kTile;
+    const double* src = (I < J)    ? ws + g.tile_off(I, J)
+                        : (I == J) ? ws + g.m_offset() + (size_t)J * kTile
+                                   : ws + g.p_offset() + (size_t)J * kTile;
     bulk_g2s(slot + I * kTile, src, kTile * sizeof(double), bar);
   }
 }
@@ -591,26 +601,39 @@ __device__ void chain_cta(const Geo& g, const double* S, double* ws, double* x, 
   __syncthreads();
   auto parity = [&](int J) { return (unsigned)(((nblk - 1 - J) / R) & 1); };
   const bool write_x = *(volatile int*)solve_ok != 0;  // every pivot is known by now
+  // x_J = M_J (t_J - L_{J+1,J}^T x_{J+1}) = M_J t_J - P_J x_{J+1}: warp 9
+  // forms v_J = M_J t_J (t_J holds every term but x_{J+1}'s by now) while
+  // warp 0 forms P_J x_{J+1}, so one 16x16 product per block row lies on the
+  // chain
   for (int J = nblk - 1; J >= 0; --J) {
     const double* rowJ = slot(J);
     const double* rowJ1 = slot(J + 1);
     if (warp == 0) {
       mbar_wait(bars + J % R, parity(J), abort_word);
       const int h = lane >> 4, c = lane & 15;
-      double s = 0.0;
+      double y = 0.0;
       if (J + 1 < nblk) {
-        const double* Lt = rowJ1 + J * kTile;
+        const double* Pt = rowJ + (J + 1) * kTile;  // P_J[c][q] at [q * 16 + c]
         const double* xj = xs + kB * (J + 1);
         double p0 = 0.0, p1 = 0.0;
 #pragma unroll
         for (int q = 0; q < 8; q += 2) {
-          p0 = fma(Lt[(8 * h + q) * kB + c], xj[8 * h + q], p0);
-          p1 = fma(Lt[(8 * h + q + 1) * kB + c], xj[8 * h + q + 1], p1);
+          p0 = fma(Pt[(8 * h + q) * kB + c], xj[8 * h + q], p0);
+          p1 = fma(Pt[(8 * h + q + 1) * kB + c], xj[8 * h + q + 1], p1);
         }
-        s = p0 + p1;
-        s += __shfl_xor_sync(0xffffffffu, s, 16);
+        y = p0 + p1;
+        y += __shfl_xor_sync(0xffffffffu, y, 16);
       }
-      const double u = t[kB * J + c] - s;
+      bar_sync(kBarBack, 64);  // v_J is in t's row J
+      if (lane < kB) {
+        const double xv = t[kB * J + c] - y;
+        xs[kB * J + c] = xv;
+        if (kB * J + c < g.n && write_x) x[kB * J + c] = xv;
+      }
+    } else if (warp == 9) {
+      mbar_wait(bars + J % R, parity(J), abort_word);
+      const int h = lane >> 4, c = lane & 15;
+      const double u = t[kB * J + c];
       const double* Ms = rowJ + J * kTile;
       double p0 = 0.0, p1 = 0.0;
 #pragma unroll
@@ -620,12 +643,10 @@ __device__ void chain_cta(const Geo& g, const double* S, double* ws, double* x, 
         p0 = fma(Ms[(8 * h + q) * kB + c], u0, p0);
         p1 = fma(Ms[(8 * h + q + 1) * kB + c], u1, p1);
       }
-      double xv = p0 + p1;
-      xv += __shfl_xor_sync(0xffffffffu, xv, 16);
-      if (lane < kB) {
-        xs[kB * J + c] = xv;
-        if (kB * J + c < g.n && write_x) x[kB * J + c] = xv;
-      }
+      double v = p0 + p1;
+      v += __shfl_xor_sync(0xffffffffu, v, 16);
+      if (lane < kB) t[kB * J + c] = v;
+      bar_arrive(kBarBack, 64);
     } else if (warp < 8 && warp != 4) {
       // warp 4 shares warp 0's sub-partition and stays out of the FP64 work
       if (J + 1 < nblk) {
@@ -667,7 +688,8 @@ __device__ void chain_cta(const Geo& g, const double* S, double* ws, double* x, 
 //   update (i, j, s): inputs tile (i, j) at version s, W_is, L_js; result to
 //                 tile (i, j) (lower part of a diagonal tile, row 0 of the
 //                 right-hand side), flag (i, j) = s+1
-//   inverse J:    input L_JJ; M_J to its slot, inverse flag J = 1
+//   inverse J:    inputs L_JJ and L_{J+1,J}; M_J = L_JJ^-T and
+//                 P_J = M_J L_{J+1,J}^T to theirs, inverse flag J = 1
 //   lookahead (r, s+1, s), right after panel (r, s), r = s+2: step s on
 //                 tiles (r, s+1) and (r, r) with W and L of that panel; the
 //                 two tiles are the chain CTA's inputs for step s+1 and go
@@ -730,8 +752,9 @@ __device__ void load_task(const Geo& g, const double* S, const double* ws, int* 
     // the chain CTA releases its panel after arming the mbarrier the pushes
     // count on and after its last read of the buffers they overwrite
     if (lane == 2) f = flag_at(fl, nblk, j, s), v = s + 1, guard = true;
-  } else {  // diagonal tile i factored
+  } else {  // diagonal tile i factored, the chain's panel (i+1, i)
     if (lane == 0) f = flag_at(fl, nblk, i, i), v = i + 1;
+    if (lane == 1 && i + 1 < nblk) f = flag_at(fl, nblk, i + 1, i), v = i + 1;
   }
   if (f) wait_ge(f, v, abort_word, guard);
   __syncwarp();
@@ -749,6 +772,7 @@ __device__ void load_task(const Geo& g, const double* S, const double* ws, int* 
     stage_tile(g, S, ws, s, j, 1, st + kStL, kPad, false);
   } else {
     stage_tile(g, S, ws, i, i, 1, st + kStW, kPad, false);
+    if (i + 1 < nblk) stage_tile(g, S, ws, i, i + 1, 1, st + kStL, kPad, false);  // L_{i+1,i}
   }
 }
 
@@ -809,9 +833,22 @@ __device__ void math_task(const Geo& g, const double* st, double* out, const dou
     }
   } else {
     // M_J = L_JJ^-T, the panel solve of the identity, stored transposed
-    // (M_J[c][q] at [q * 16 + c])
+    // (M_J[c][q] at [q * 16 + c]); then P_J = M_J L_{J+1,J}^T, stored the
+    // same way, into the second half
     const int row = 2 * warp + (lane >> 4), c = lane & 15;
     out[c * kB + row] = fwd_rows(row == c ? 1.0 : 0.0, Lk, lane);
+    if (i + 1 < g.nblk) {
+      bar_sync(kBarMath, kMath);
+      const int q = tid >> 4, cc = tid & 15;
+      const double* lq = st + kStL + q * kPad;  // row q of L_{J+1,J}
+      double p0 = 0.0, p1 = 0.0;
+#pragma unroll
+      for (int r = 0; r < kB; r += 2) {
+        p0 = fma(out[r * kB + cc], lq[r], p0);
+        p1 = fma(out[(r + 1) * kB + cc], lq[r + 1], p1);
+      }
+      out[kTile + tid] = p0 + p1;
+    }
   }
 }
 
@@ -855,6 +892,9 @@ __device__ void store_task(const Geo& g, double* ws, int* fl, const double* out,
       const int e = 2 * (lane + 32 * u);
       __stcg(reinterpret_cast<double2*>(ws + g.m_offset() + (size_t)i * kTile + e),
              *reinterpret_cast<const double2*>(out + e));
+      if (i + 1 < nblk)
+        __stcg(reinterpret_cast<double2*>(ws + g.p_offset() + (size_t)i * kTile + e),
+               *reinterpret_cast<const double2*>(out + kTile + e));
     }
     f = fl + g.inv_index(i);
     v = 1;

@@ -113,7 +113,7 @@ struct Bufs {
   void* ppart;      // [npchunk][36] accumulators
   void* qpart;      // [nchunk][6] accumulators of Hpl Dinv b_l per pose chunk
   double* S;        // [(ld+32) x ld]
-  double* cws;      // [(ld+32) x ld] workspace of the cluster factorisation
+  double* cws;      // workspace of the cluster or tiled factorisation
   double* dinv;     // [ld] reciprocal Cholesky diagonal
   double* x;        // [6Kf + 3Lf]
   double* cost_part;
@@ -1959,7 +1959,7 @@ int alloc_numerics(Solver* s, std::string* err) {
   CK(s->ppart.ensure(std::max<size_t>(1, (size_t)L.npc * 36 * ab)));
   CK(s->qpart.ensure(std::max<size_t>(1, (size_t)L.nchunk * 6 * ab)));
   CK(s->S.ensure((size_t)(L.ld + kNB) * L.ld));
-  CK(s->cws.ensure(std::max((size_t)(L.ld + kNB) * L.ld, chol_tiled_ws_doubles(L.ld))));
+  CK(s->cws.ensure(std::max(chol_cluster_ws_doubles(L.ld, L.n), chol_tiled_ws_doubles(L.ld))));
   CK(s->dinv.ensure(L.ld));
   CK(s->x.ensure(std::max(nx, 1)));
   CK(s->cost_part.ensure(L.ncost));
@@ -2511,7 +2511,7 @@ bool window_descs(Solver* const* ss, const std::vector<int>& order, const RunOpt
     d.NP = L.NP;
     d.max_log = std::max(1, o.iterations * o.max_trials);
     const int nb = (L.n + chold::kB - 1) / chold::kB;
-    if (L.Kf && (nb > chold::kMaxBlk || chold::make_geo(16, L.ld, L.n, 1).ws_doubles() > (size_t)(L.ld + kNB) * L.ld)) {
+    if (L.Kf && nb > chold::kMaxBlk) {
       if (err) *err = "a window's reduced camera system exceeds the persistent batch's limit (384 unknowns)";
       return false;
     }

@@ -3,7 +3,8 @@
 // (1..384 unknowns) and every backward-solve slot count, the bulk-copy
 // targets and sources are 16-byte aligned, the mbarriers 8-byte aligned, the
 // flag array lies past everything the chain CTA uses, the workspace fits
-// the (ld + 32) x ld buffer the solver provides, and the slot count the plan
+// the buffer the solver provides (chol_cluster_ws_doubles), and the slot
+// count the plan
 // picks for the largest opt-in shared memory of the part (227 KB) leaves at
 // least three slots.  Built and run by tests/test_chol_layout.py.
 #include "mcba_chol.cu"
@@ -24,8 +25,9 @@ int main() {
     for (int C : {16, 8, 4}) {
       for (int R = 1; R <= nblk; ++R) {
         const Geo g = make_geo(C, ld, n, R);
-        if (g.ws_doubles() > (size_t)(ld + 32) * ld) fail("workspace exceeds (ld + 32) x ld", n, R);
-        if (g.tile_off(1, 0) % 2 || g.m_offset() % 2) fail("workspace tile not 16-byte aligned", n, R);
+        if (g.ws_doubles() > chol_cluster_ws_doubles(ld, n)) fail("workspace exceeds the solver's buffer", n, R);
+        if (g.tile_off(1, 0) % 2 || g.m_offset() % 2 || g.p_offset() % 2)
+          fail("workspace tile not 16-byte aligned", n, R);
         for (int s = 0; s <= R; ++s)
           if (g.b_slot(s) % 2) fail("backward slot not 16-byte aligned", n, R);
         if (g.c_p(0) % 2 || g.c_diag(1) % 2) fail("push target not 16-byte aligned", n, R);

@@ -13,14 +13,14 @@ extern "C" int chol_probe_solve(const double* S_host, int n, int ld, double* x_h
   using namespace mcba;
   CholPlan plan;
   if (!chol_cluster_plan(ld, n, &plan)) return -1;
-  const size_t total = (size_t)(ld + 32) * ld;
+  const size_t total = (size_t)(ld + 32) * ld, wtotal = chol_cluster_ws_doubles(ld, n);
   double *S = nullptr, *ws = nullptr, *x = nullptr;
   int* ok = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   int rc = 0;
   const int one = 1;
   // every early exit below goes through the frees at the end
-  if (cudaMalloc(&S, total * sizeof(double)) != cudaSuccess || cudaMalloc(&ws, total * sizeof(double)) != cudaSuccess ||
+  if (cudaMalloc(&S, total * sizeof(double)) != cudaSuccess || cudaMalloc(&ws, wtotal * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&x, (size_t)ld * sizeof(double)) != cudaSuccess || cudaMalloc(&ok, sizeof(int)) != cudaSuccess) {
     rc = -2;
   } else if (cudaMemcpy(S, S_host, total * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||

@@ -104,6 +104,7 @@ def emulate(n, C, seed):
     ws = np.full((ld + 32, ld), np.nan)  # rows ld+1, ld+2: 1/d and y
     fl = {}
     Ms = {}
+    Ps = {}
 
     def flag(key):
         return fl.get(key, 0)
@@ -125,8 +126,9 @@ def emulate(n, C, seed):
     assert set(allt) == expected_tasks(nblk)
 
     def ready(t):  # load_task's flag conditions
-        if t[0] == "inv":
-            return flag((t[1], t[1])) >= t[1] + 1
+        if t[0] == "inv":  # diagonal tile J factored, the chain's panel (J+1, J)
+            J = t[1]
+            return flag((J, J)) >= J + 1 and (J + 1 == nblk or flag((J + 1, J)) >= J + 1)
         if t[0] == "panel":
             _, i, k = t
             return (k == 0 or flag((i, k)) >= k) and flag((k, k)) >= k + 1
@@ -138,6 +140,10 @@ def emulate(n, C, seed):
             J = t[1]
             Lu = np.tril(ws[tile(J, J)], -1) + np.eye(B)
             Ms[J] = np.linalg.inv(Lu).T
+            if J + 1 < nblk:  # P_J = M_J L_{J+1,J}^T
+                Lt = ws[upper(J + 1, J)].copy()
+                assert not np.isnan(Lt).any(), ("inverse reads an unwritten panel", J)
+                Ps[J] = Ms[J] @ Lt.T
             fl[("inv", J)] = 1
             return
         if t[0] == "panel":
@@ -207,11 +213,17 @@ def emulate(n, C, seed):
             t = ws[ld + 2, :B * nblk].copy()
             t[B * (nblk - 1):] = st["ylast"]
             x = np.zeros(B * nblk)
+            # row J: x_J = M_J t_J - P_J x_{J+1}, t_J holding every term
+            # but x_{J+1}'s; x_{J+1}'s terms of the rows above J come off
+            # in the same step
             for J in range(nblk - 1, -1, -1):
                 xJ = Ms[J] @ t[B * J:B * J + B]
+                if J + 1 < nblk:
+                    x1 = x[B * (J + 1):B * (J + 2)]
+                    xJ = xJ - Ps[J] @ x1
+                    for I in range(J):
+                        t[B * I:B * I + B] -= ws[upper(J + 1, I)].T @ x1
                 x[B * J:B * J + B] = xJ
-                for I in range(J):
-                    t[B * I:B * I + B] -= ws[upper(J, I)].T @ xJ
             st["x"] = x
             st["phase"] = "done"
             return True
