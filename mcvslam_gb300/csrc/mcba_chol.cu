@@ -25,7 +25,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_ldlt_cluster(const double* S, d
 }  // namespace
 
 size_t chol_cluster_ws_doubles(int ld, int n) {
-  return std::max((size_t)(ld + 32) * ld, make_geo(16, ld, n, 1).ws_doubles());
+  return std::max((size_t)(ld + 32) * ld, make_geo(16, ld, n).ws_doubles());
 }
 
 int chol_cluster_plan(int ld, int n, CholPlan* plan) {
@@ -43,17 +43,13 @@ int chol_cluster_plan(int ld, int n, CholPlan* plan) {
     cudaGetLastError();
     return 0;
   }
-  // as many backward-solve row slots as fit (all rows when possible), at
-  // least three
-  int R = nblk;
-  while (R > std::min(nblk, 3) && make_geo(16, ld, n, R).total() * sizeof(double) + reserve > (size_t)max_smem) --R;
   // cluster size by the work: a chain CTA, the lookahead worker and enough
   // general workers for the trailing updates (small systems, e.g. the
   // windows of a batch that run side by side, take fewer SMs)
   const int Cpref = nblk >= 10 ? 16 : (nblk >= 5 ? 8 : 4);
   for (int C : {16, 8, 4}) {
     if (C > Cpref) continue;
-    const Geo g = make_geo(C, ld, n, R);
+    const Geo g = make_geo(C, ld, n);
     const size_t bytes = g.total() * sizeof(double);
     if (bytes + reserve > (size_t)max_smem) continue;
     cudaLaunchConfig_t cfg = {};
@@ -74,7 +70,6 @@ int chol_cluster_plan(int ld, int n, CholPlan* plan) {
     }
     plan->ok = true;
     plan->cluster = C;
-    plan->slots = R;
     plan->smem_bytes = bytes;
     return 1;
   }
@@ -83,7 +78,7 @@ int chol_cluster_plan(int ld, int n, CholPlan* plan) {
 
 cudaError_t chol_cluster_launch(const CholPlan& plan, const double* S, double* ws, int ld, int n, double* x,
                                 int* solve_ok, cudaStream_t st) {
-  const Geo g = make_geo(plan.cluster, ld, n, plan.slots);
+  const Geo g = make_geo(plan.cluster, ld, n);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(plan.cluster, 1, 1);
   cfg.blockDim = dim3(kThreads, 1, 1);

@@ -10,13 +10,12 @@ namespace mcba {
 struct CholPlan {
   bool ok = false;
   int cluster = 0;
-  int slots = 0;  // backward-solve row slots held in shared memory
   size_t smem_bytes = 0;
 };
 
-// Chooses a cluster size (16, 8 or 4 CTAs by the size) for the n x n system (row stride ld)
-// and the number of backward-solve rows staged in shared memory; returns 0
-// (plan.ok = false) when the system is too large for the cluster solve.
+// Chooses a cluster size (16, 8 or 4 CTAs by the size) for the n x n system
+// (row stride ld); returns 0 (plan.ok = false) when the system is too large
+// for the cluster solve.
 int chol_cluster_plan(int ld, int n, CholPlan* plan);
 
 // Doubles of the workspace chol_cluster_launch needs for the n x n system

@@ -53,19 +53,21 @@
 //     whichever die the flag's line maps to, and the factorisation time
 //     depended on that (98 or 104 us at n = 168 on GB300, by the page).
 //   * Backward solve L^T x = y on the chain CTA, block row by block row:
-//     rows of L, M and P arrive in shared memory by bulk asynchronous copies
-//     (one per tile), and per block row only one 16x16 product lies on the
-//     dependency chain (x_J = M_J t_J - P_J x_{J+1}, with P_J =
-//     M_J L_{J+1,J}^T formed beside M_J by the lookahead worker and M_J t_J
-//     by a second warp).
+//     per block row only one 16x16 product lies on the dependency chain
+//     (x_J = M_J t_J - P_J x_{J+1}, with P_J = M_J L_{J+1,J}^T formed beside
+//     M_J by the lookahead worker and M_J t_J by a second warp); six helper
+//     warps apply the other terms of t as the rows of x appear, handing over
+//     through counters in shared memory, and every warp loads its tiles
+//     from L2 into registers two uses ahead.
 //
 // Every wait has a time limit (%globaltimer); a wait that runs out sets an
 // abort word, and the solve then reports failure (*solve_ok = 0) instead of
 // hanging.  Waits on the workers' flags end at once when the abort word is
-// set.  The waits that guard shared memory (the pushes into the chain CTA,
-// the chain CTA's own bulk copies, and the lookahead worker's wait for the
-// chain CTA's panel, which orders its pushes after the chain CTA's
-// mbarrier arms) run to completion even then: their producers run whatever
+// set.  The waits that guard shared memory (the pushes into the chain CTA
+// and the lookahead worker's wait for the chain CTA's panel, which orders
+// its pushes after the chain CTA's mbarrier arms) run to completion even
+// then, as do the chain CTA's waits on its own warps: their producers run
+// whatever
 // the other flags say, so no copy into shared memory is in flight when a CTA
 // leaves.  A pivot <= 0 clears *solve_ok; the
 // chain CTA, which factors every diagonal tile, then leaves x untouched.
@@ -108,7 +110,7 @@ constexpr int kBarOutFull = 4;  // workers: result buffer b ready for warp 8, id
 constexpr int kBarOutFree = 6;  // workers: result buffer b stored, ids 6, 7
 constexpr int kBarInFull = 8;   // workers: inputs of the next task staged by warp 9, ids 8, 9
 constexpr int kBarInFree = 10;  // workers: stage b read by warps 0-7, ids 10, 11
-constexpr int kBarBack = 12;    // chain CTA, backward solve: warp 9's M_J t_J ready for warp 0
+constexpr int kHelpers = 6;     // chain CTA, backward solve: warps 1-3 and 5-7 apply the terms of t
 
 // Reciprocal of a pivot: rcp.approx.ftz.f64 (relative error ~1e-6), then one
 // cubic Newton-Raphson step y (1 + e + e^2), e = 1 - d y, which leaves an
@@ -157,20 +159,8 @@ __device__ __forceinline__ void mbar_inval(uint64_t* bar) {
 
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async;" ::: "memory"); }
-
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-
-// Bulk asynchronous copy global -> this CTA's shared memory, completion
-// counted in bytes on the mbarrier (addresses 16-byte aligned, size a
-// multiple of 16).
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   smem_u32(dst)),
-               "l"(src), "r"(bytes), "r"(smem_u32(bar))
-               : "memory");
 }
 
 // This CTA's shared-memory address of `local`'s offset in cluster CTA `rank`.
@@ -194,16 +184,6 @@ __device__ __forceinline__ bool mbar_try_wait_cluster(uint64_t* bar, unsigned pa
   asm volatile(
       "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, "
       "p;\n}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
-  unsigned ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
       : "=r"(ok)
       : "r"(smem_u32(bar)), "r"(parity)
       : "memory");
@@ -241,12 +221,25 @@ __device__ bool wait_ge(const int* p, int v, int* abort_word, bool guard = false
   return false;
 }
 
-// Bounded wait for an mbarrier phase that only this CTA's own bulk copies
-// complete: copies always land, so it waits whatever the abort word says.
-__device__ void mbar_wait(uint64_t* bar, unsigned parity, int* abort_word) {
+// Counters in this CTA's shared memory that its warps hand over through
+// (release / acquire at CTA scope).
+__device__ __forceinline__ void st_local(int* p, int v) {
+  asm volatile("st.release.cta.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(p)), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ int ld_local(const int* p) {
+  int v;
+  asm volatile("ld.acquire.cta.shared::cta.b32 %0, [%1];" : "=r"(v) : "r"(smem_u32(p)) : "memory");
+  return v;
+}
+
+// Bounded wait (every lane of a warp may call it) for *p >= v, a counter
+// that another warp of this CTA advances whatever the abort word says; a
+// wait that runs out sets the abort word.
+__device__ void wait_local(const int* p, int v, int* abort_word) {
   unsigned long long t0 = 0;
   for (unsigned it = 0; it < kPollCap; ++it) {
-    if (mbar_try_wait(bar, parity)) return;
+    if (ld_local(p) >= v) return;
     if ((it & 63u) == 0) {
       const unsigned long long t = now_ns();
       if (it == 0)
@@ -276,9 +269,9 @@ __device__ void mbar_wait_cluster(uint64_t* bar, unsigned parity, int* abort_wor
 }
 
 struct Geo {
-  int C, nblk, ld, n, R;  // R: backward-solve row slots in shared memory
-  int hold;               // a flag the workers leave unreleased (-1 in every solve; the test of the
-                          // bounded waits sets it so that a wait runs out)
+  int C, nblk, ld, n;
+  int hold;  // a flag the workers leave unreleased (-1 in every solve; the test of the bounded waits
+             // sets it so that a wait runs out)
   // workspace (doubles): nblk x nblk tiles of 256, then the right-hand-side
   // rows W, 1/d and y (16 nblk each), then the inverses M_J (256 each,
   // transposed), then the products P_J = M_J L_{J+1,J}^T (256 each,
@@ -308,14 +301,13 @@ struct Geo {
   __host__ __device__ size_t c_lk() const { return c_lp() + kPadTile; }
   __host__ __device__ size_t c_rx(int b) const { return c_lk() + kPadTile + kB + b; }
   __host__ __device__ size_t c_end() const { return c_rx(2); }
-  // backward solve, after that: t, x, the slot mbarriers, R row slots of
-  // nblk tiles (row J: L_JI at positions I < J, M_J at J, P_J at J+1; the
-  // last row has no P)
+  // backward solve, after that: t, x, the counters its warps hand over
+  // through (ints) and M of the last diagonal tile
   __host__ __device__ size_t b_t() const { return c_end(); }
   __host__ __device__ size_t b_x() const { return b_t() + (size_t)kB * nblk; }
-  __host__ __device__ size_t b_bar() const { return b_x() + (size_t)kB * nblk; }
-  __host__ __device__ size_t b_slot(int s) const { return b_bar() + (size_t)((R + 1) & ~1) + (size_t)s * nblk * kTile; }
-  __host__ __device__ size_t b_end() const { return b_slot(R); }
+  __host__ __device__ size_t b_fl() const { return b_x() + (size_t)kB * nblk; }
+  __host__ __device__ size_t b_mlast() const { return b_fl() + (size_t)((((2 + nblk) + 1) / 2 + 1) & ~1); }
+  __host__ __device__ size_t b_end() const { return b_mlast() + kTile; }
   // worker: two input stages (A, then W or L_kk, then L or 1/d) and two
   // result buffers of 512
   __host__ __device__ size_t w_stage(int b) const { return (size_t)b * (kTile + 2 * kPadTile); }
@@ -407,31 +399,13 @@ __device__ void diag_ldlt(double* T, double* rd, double* sq, int* solve_ok) {
   }
 }
 
-// One backward-solve row J into a shared-memory slot by bulk asynchronous
-// copies, one per tile: L_JI (I < J) into positions I, and, unless the chain
-// CTA computed M_J in place (the last row), M_J into position J and P_J into
-// position J+1.  Run by one whole warp once every producer is known to be
-// done.
-__device__ void issue_row(const Geo& g, const double* ws, double* slot, uint64_t* bar, int J, bool with_m) {
-  const int lane = threadIdx.x & 31;
-  const int ncopy = J + (with_m ? 2 : 0);
-  if (lane == 0) mbar_expect_tx(bar, (unsigned)ncopy * kTile * sizeof(double));
-  __syncwarp();
-  for (int I = lane; I < ncopy; I += 32) {
-    const double* src = (I < J)    ? ws + g.tile_off(I, J)
-                        : (I == J) ? ws + g.m_offset() + (size_t)J * kTile
-                                   : ws + g.p_offset() + (size_t)J * kTile;
-    bulk_g2s(slot + I * kTile, src, kTile * sizeof(double), bar);
-  }
-}
-
 // ------------------------------------------------------------ chain CTA --
 
 __device__ void chain_cta(const Geo& g, const double* S, double* ws, double* x, int* solve_ok, int* fl,
                           double* sm) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int rr = (tid >> 4) & 15, cc = tid & 15;
-  const int nblk = g.nblk, ld = g.ld, R = g.R;
+  const int nblk = g.nblk, ld = g.ld;
   int* abort_word = fl + g.abort_index();
   double* const Tb0 = sm + g.c_diag(0);
   double* const Tb1 = sm + g.c_diag(1);
@@ -442,14 +416,9 @@ __device__ void chain_cta(const Geo& g, const double* S, double* ws, double* x, 
   double* Lk = sm + g.c_lk();
   double* t = sm + g.b_t();
   double* xs = sm + g.b_x();
-  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + g.b_bar());
-  auto slot = [&](int J) { return sm + g.b_slot(J % R); };
+  double* const Mlast = sm + g.b_mlast();
   int cur = 0;
   if (tid < kMath) Tb0[tid] = __ldcg(S + (size_t)rr * ld + cc);
-  if (tid == kMath) {
-    for (int b = 0; b < R; ++b) mbar_init(bars + b, 1);
-    fence_mbar_init();
-  }
   __syncthreads();
 
   for (int k = 0; k + 1 < nblk; ++k) {
@@ -539,7 +508,7 @@ __device__ void chain_cta(const Geo& g, const double* S, double* ws, double* x, 
 
   // ---- last diagonal tile: factor it; warp 8 fetches the last
   //      right-hand-side tile meanwhile.  Then M = L^-T of the tile goes
-  //      straight into its backward-solve slot and the last y into t.
+  //      to shared memory for the backward solve and the last y into t.
   {
     const int k = nblk - 1;
     double* T = cur ? Tb1 : Tb0;
@@ -563,115 +532,196 @@ __device__ void chain_cta(const Geo& g, const double* S, double* ws, double* x, 
     if (warp < 8) {
       const int row = 2 * warp + (lane >> 4), c = lane & 15;
       const double m = fwd_rows(row == c ? 1.0 : 0.0, Lk, lane);
-      slot(k)[k * kTile + c * kB + row] = m;  // M_k stored transposed
+      Mlast[c * kB + row] = m;  // M_k stored transposed
     } else if (warp == 8) {
       const double a = fwd_rows(lane < kB ? P[lane] : 0.0, Lk, lane);
       if (lane < kB) t[kB * k + lane] = a * Lk[kPadTile + lane];
     }
   }
 
-  // ---- backward solve L^T x = y, block row by block row.  Rows reach
-  //      shared memory by bulk copies, R slots deep; per row J:
-  //        warp 0:     u = t_J - L_{J+1,J}^T x_{J+1};  x_J = M_J u
-  //        warps 1-3, 5-7:  t_I -= L_{J+1,I}^T x_{J+1}, I <= J-1
-  //        warp 8:     issues row J+2-R
-  //      so only the two 16x16 products of warp 0 lie on the chain.
+  // ---- backward solve L^T x = y, block row by block row, as a dataflow
+  //      inside the chain CTA.  x_J = M_J t_J - P_J x_{J+1}, where t_J must
+  //      hold y_J minus the terms L_KJ^T x_K of every K >= J+2:
+  //        warps 1-3, 5-7 (helpers): helper h owns the rows I = h mod 6 of
+  //                 t and applies x_K's terms to them as x_K appears (K
+  //                 descending; row K-2, needed next, first), then marks
+  //                 row K-2 ready
+  //        warp 9:  v_J = M_J t_J into t's row J once row J is ready
+  //        warp 0:  P_J x_{J+1}, then x_J = v_J - P_J x_{J+1}
+  //      The warps hand over through counters in shared memory (release /
+  //      acquire at CTA scope): rows of x published, rows of v formed and a
+  //      ready mark per row.  Each warp loads the tiles it multiplies by
+  //      (P_J, M_J, L_KI) from L2 straight into registers, two rows (warps
+  //      0 and 9) or one term (helpers) ahead of their use, so no copy into
+  //      shared memory paces the rows (bulk copies of the rows into shared
+  //      memory took ~1.1 us a row to issue and land).  Every producer of
+  //      the counters runs inside the CTA whatever the abort word says, so
+  //      their waits do not end on it.
   //      Right-hand-side panel J is done only after every L_JI was (its
   //      updates read them), and the last right-hand-side tile waited above
   //      covers row nblk-1; so warp 8 waits for the right-hand-side panels
-  //      and the inverses, one lane per row, then issues rows.  Issuing a
-  //      row's copies takes ~0.45 us (one bulk copy per tile), so with four
-  //      or more slots only the first two rows are issued here and row J-2
-  //      in iteration J, two iterations ahead of its use and into the slot
-  //      of a row already done; with three slots, the first three here and
-  //      row J+2-R in iteration J.
-  const int ahead = R >= 4 ? 2 : R;
+  //      and the inverses, one lane per row, before anything is read.
+  int* const xcnt = reinterpret_cast<int*>(sm + g.b_fl());
+  int* const vcnt = xcnt + 1;
+  int* const ready = xcnt + 2;
   if (warp == 8) {
     if (lane < nblk - 1) {
       wait_ge(flag_at(fl, nblk, nblk, lane), lane + 1, abort_word);
       wait_ge(fl + g.inv_index(lane), 1, abort_word);
     }
-    __syncwarp();
-    fence_proxy_async();
-    for (int J = nblk - 1; J >= 0 && J >= nblk - ahead; --J)
-      issue_row(g, ws, slot(J), bars + J % R, J, J < nblk - 1);
+  } else if (tid < 2 + nblk) {
+    xcnt[tid] = 0;
   }
   __syncthreads();
+  const int h = lane >> 4, c = lane & 15;
+  // lane (h, c)'s eight elements of a transposed tile in the workspace
+  // (global memory): [(8h + q) * 16 + c]
+  auto load8 = [&](double* r, const double* tile) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) r[q] = __ldcg(tile + (8 * h + q) * kB + c);
+  };
+  const double* const Mg = ws + g.m_offset();
+  const double* const Pg = ws + g.p_offset();
+  // three register tiles per warp, in rotation: each load is made two rows
+  // (or two terms) ahead of its use and used where it landed
+  double b0[8] = {}, b1[8] = {}, b2[8] = {};
+  // warp 0: P_{nblk-2} and P_{nblk-3}; warp 9: M_{nblk-2} and M_{nblk-3}
+  // (M_{nblk-1} the chain CTA formed in shared memory)
+  if (warp == 0 || warp == 9) {
+    const double* base = warp == 0 ? Pg : Mg;
+    if (nblk >= 2) load8(b0, base + (size_t)(nblk - 2) * kTile);
+    if (nblk >= 3) load8(b1, base + (size_t)(nblk - 3) * kTile);
+  }
   for (int e = tid; e < kB * (nblk - 1); e += kThreads) t[e] = __ldcg(ws + g.rhs_y() + e);
   __syncthreads();
-  auto parity = [&](int J) { return (unsigned)(((nblk - 1 - J) / R) & 1); };
   const bool write_x = *(volatile int*)solve_ok != 0;  // every pivot is known by now
-  // x_J = M_J (t_J - L_{J+1,J}^T x_{J+1}) = M_J t_J - P_J x_{J+1}: warp 9
-  // forms v_J = M_J t_J (t_J holds every term but x_{J+1}'s by now) while
-  // warp 0 forms P_J x_{J+1}, so one 16x16 product per block row lies on the
-  // chain
-  for (int J = nblk - 1; J >= 0; --J) {
-    const double* rowJ = slot(J);
-    const double* rowJ1 = slot(J + 1);
-    if (warp == 0) {
-      mbar_wait(bars + J % R, parity(J), abort_word);
-      const int h = lane >> 4, c = lane & 15;
+  if (warp == 0) {
+    // x_J = v_J - P_J x_{J+1} (no P for the last row)
+    auto row = [&](const double(&Pr)[8], int J) {
       double y = 0.0;
       if (J + 1 < nblk) {
-        const double* Pt = rowJ + (J + 1) * kTile;  // P_J[c][q] at [q * 16 + c]
         const double* xj = xs + kB * (J + 1);
         double p0 = 0.0, p1 = 0.0;
 #pragma unroll
         for (int q = 0; q < 8; q += 2) {
-          p0 = fma(Pt[(8 * h + q) * kB + c], xj[8 * h + q], p0);
-          p1 = fma(Pt[(8 * h + q + 1) * kB + c], xj[8 * h + q + 1], p1);
+          p0 = fma(Pr[q], xj[8 * h + q], p0);
+          p1 = fma(Pr[q + 1], xj[8 * h + q + 1], p1);
         }
         y = p0 + p1;
         y += __shfl_xor_sync(0xffffffffu, y, 16);
       }
-      bar_sync(kBarBack, 64);  // v_J is in t's row J
+      wait_local(vcnt, nblk - J, abort_word);  // v_J is in t's row J
       if (lane < kB) {
         const double xv = t[kB * J + c] - y;
         xs[kB * J + c] = xv;
         if (kB * J + c < g.n && write_x) x[kB * J + c] = xv;
       }
-    } else if (warp == 9) {
-      mbar_wait(bars + J % R, parity(J), abort_word);
-      const int h = lane >> 4, c = lane & 15;
+      __syncwarp();
+      if (lane == 0) st_local(xcnt, nblk - J);
+    };
+    // row J with P_J in cur; P_{J-2} into pre
+    auto step = [&](const double(&cur)[8], double(&pre)[8], int J) {
+      if (J < 0) return false;
+      if (J >= 2) load8(pre, Pg + (size_t)(J - 2) * kTile);
+      row(cur, J);
+      return true;
+    };
+    row(b2, nblk - 1);
+    for (int J = nblk - 2; step(b0, b2, J) && step(b1, b0, J - 1) && step(b2, b1, J - 2); J -= 3) {
+    }
+  } else if (warp == 9) {
+    // v_J = M_J t_J into t's row J once row J is ready
+    auto row = [&](const double(&Mr)[8], int J) {
+      if (J + 2 < nblk) wait_local(ready + J, 1, abort_word);
       const double u = t[kB * J + c];
-      const double* Ms = rowJ + J * kTile;
       double p0 = 0.0, p1 = 0.0;
 #pragma unroll
       for (int q = 0; q < 8; q += 2) {
         const double u0 = __shfl_sync(0xffffffffu, u, 8 * h + q);
         const double u1 = __shfl_sync(0xffffffffu, u, 8 * h + q + 1);
-        p0 = fma(Ms[(8 * h + q) * kB + c], u0, p0);
-        p1 = fma(Ms[(8 * h + q + 1) * kB + c], u1, p1);
+        p0 = fma(Mr[q], u0, p0);
+        p1 = fma(Mr[q + 1], u1, p1);
       }
       double v = p0 + p1;
       v += __shfl_xor_sync(0xffffffffu, v, 16);
       if (lane < kB) t[kB * J + c] = v;
-      bar_arrive(kBarBack, 64);
-    } else if (warp < 8 && warp != 4) {
-      // warp 4 shares warp 0's sub-partition and stays out of the FP64 work
-      if (J + 1 < nblk) {
-        const double* xj = xs + kB * (J + 1);
-        for (int it = tid - (warp < 4 ? 32 : 64); it < kB * J; it += kMath - 64) {
-          const int I = it >> 4, c = it & 15;
-          const double* Tm = rowJ1 + I * kTile;
-          double v0 = 0.0, v1 = 0.0;
+      __syncwarp();
+      if (lane == 0) st_local(vcnt, nblk - J);
+    };
+    auto step = [&](const double(&cur)[8], double(&pre)[8], int J) {
+      if (J < 0) return false;
+      if (J >= 2) load8(pre, Mg + (size_t)(J - 2) * kTile);
+      row(cur, J);
+      return true;
+    };
+    {  // M_{nblk-1} from shared memory
+      const double* Ms = Mlast;
 #pragma unroll
-          for (int q = 0; q < kB; q += 2) {
-            v0 = fma(Tm[q * kB + c], xj[q], v0);
-            v1 = fma(Tm[(q + 1) * kB + c], xj[q + 1], v1);
-          }
-          t[kB * I + c] -= v0 + v1;
-        }
-      }
-    } else if (warp == 8) {
-      const int Jn = R >= 4 ? J - 2 : J + 2 - R;
-      if (Jn >= 0 && Jn < nblk - ahead) {
-        fence_proxy_async();  // the slot's earlier reads come before the copies into it
-        issue_row(g, ws, slot(Jn), bars + Jn % R, Jn, true);
-      }
+      for (int q = 0; q < 8; ++q) b2[q] = Ms[(8 * h + q) * kB + c];
+      row(b2, nblk - 1);
     }
-    __syncthreads();
+    for (int J = nblk - 2; step(b0, b2, J) && step(b1, b0, J - 1) && step(b2, b1, J - 2); J -= 3) {
+    }
+  } else if (warp != 4 && warp != 8) {
+    // warp 4 shares warp 0's sub-partition and stays out of the FP64 work
+    const int hw = warp < 4 ? warp - 1 : warp - 2;  // helper 0..5: sub-partitions 1, 2, 3, 1, 2, 3
+    // this helper's terms (K, I): K = nblk-1 .. 2, its rows I <= K-2
+    // descending; advance to the term after (K, I) (I = -1: none left)
+    auto next = [&](int& K, int& I) {
+      if (I >= kHelpers) {
+        I -= kHelpers;
+        return;
+      }
+      for (--K; K >= 2; --K)
+        if (K - 2 >= hw) {
+          I = K - 2 - (K - 2 - hw) % kHelpers;
+          return;
+        }
+      I = -1;
+    };
+    // the current term, the next two
+    int Kc = nblk, Ic = -1;
+    next(Kc, Ic);
+    int K1 = Kc, I1 = Ic;
+    if (I1 >= 0) next(K1, I1);
+    if (Ic >= 0) load8(b0, ws + g.tile_off(Ic, Kc));  // L_KI^T[c][q] at [q * 16 + c]
+    if (I1 >= 0) load8(b1, ws + g.tile_off(I1, K1));
+    int Kx = nblk;
+    double xk[8];
+    auto step = [&](const double(&cur)[8], double(&pre)[8]) {
+      if (Ic < 0) return false;
+      int K2 = K1, I2 = I1;
+      if (I2 >= 0) next(K2, I2);
+      if (I2 >= 0) load8(pre, ws + g.tile_off(I2, K2));
+      if (Kc != Kx) {  // the first term of x_K: wait for it
+        Kx = Kc;
+        wait_local(xcnt, nblk - Kc, abort_word);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) xk[q] = xs[kB * Kc + 8 * h + q];
+      }
+      double p0 = 0.0, p1 = 0.0;
+#pragma unroll
+      for (int q = 0; q < 8; q += 2) {
+        p0 = fma(cur[q], xk[q], p0);
+        p1 = fma(cur[q + 1], xk[q + 1], p1);
+      }
+      double sum = p0 + p1;
+      sum += __shfl_xor_sync(0xffffffffu, sum, 16);
+      if (lane < kB) t[kB * Ic + c] -= sum;
+      if (Ic == Kc - 2) {  // row K-2 has all its terms
+        __syncwarp();
+        if (lane == 0) st_local(ready + Ic, 1);
+      }
+      Kc = K1;
+      Ic = I1;
+      K1 = K2;
+      I1 = I2;
+      return true;
+    };
+    while (step(b0, b2) && step(b1, b0) && step(b2, b1)) {
+    }
   }
+  __syncthreads();
   if (tid == 0 && ld_acquire(abort_word) != 0) *solve_ok = 0;
 }
 
@@ -999,13 +1049,12 @@ __device__ void worker_cta(const Geo& g, const double* S, double* ws, int* fl, d
   }
 }
 
-inline Geo make_geo(int C, int ld, int n, int R) {
+inline Geo make_geo(int C, int ld, int n) {
   Geo g{};
   g.C = C;
   g.nblk = (n + kB - 1) / kB;
   g.ld = ld;
   g.n = n;
-  g.R = R;
   g.hold = -1;
   return g;
 }
@@ -1049,8 +1098,6 @@ __device__ __forceinline__ void ldlt_cluster_retire(const Geo& g, double* sm, in
   if (rank == 0 && threadIdx.x == kMath) {
     mbar_inval(reinterpret_cast<uint64_t*>(sm + g.c_rx(0)));
     mbar_inval(reinterpret_cast<uint64_t*>(sm + g.c_rx(1)));
-    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + g.b_bar());
-    for (int b = 0; b < g.R; ++b) mbar_inval(bars + b);
   }
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }

@@ -2515,10 +2515,7 @@ bool window_descs(Solver* const* ss, const std::vector<int>& order, const RunOpt
       if (err) *err = "a window's reduced camera system exceeds the persistent batch's limit (384 unknowns)";
       return false;
     }
-    int Rs = std::max(nb, 1);
-    while (Rs > std::min(nb, 3) && chold::make_geo(C, L.ld, L.n, Rs).total() * sizeof(double) + reserve > (size_t)max_smem)
-      --Rs;
-    d.g = chold::make_geo(C, L.ld, L.n, Rs);
+    d.g = chold::make_geo(C, L.ld, L.n);
     const size_t bytes = L.Kf ? d.g.total() * sizeof(double) : 0;
     if (bytes + reserve > (size_t)max_smem) {
       if (err) *err = "a window's factorisation does not fit shared memory";

@@ -30,7 +30,7 @@ extern "C" int chol_probe_solve(const double* S_host, int n, int ld, double* x_h
   } else if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
     rc = -6;
   } else {
-    Geo g = make_geo(plan.cluster, ld, n, plan.slots);
+    Geo g = make_geo(plan.cluster, ld, n);
     if (hold) g.hold = g.nblk * g.nblk;  // flag of right-hand-side panel (nblk, 0)
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(plan.cluster, 1, 1);

@@ -1,7 +1,8 @@
 """Host-side layout checks of the cluster LDL^T (tests/cpp/chol_layout.cu):
-alignment of every bulk-copy and push target, the flag array's place in the
-chain CTA's shared memory, the workspace size and the plan's slot count, for
-1..384 unknowns.  Compiled for sm_103a and run on the host; no device call."""
+alignment of the workspace tiles and push targets, the flag array's place in
+the chain CTA's shared memory, the workspace size and the shared memory
+total, for 1..384 unknowns and every cluster size.  Compiled for sm_103a and
+run on the host; no device call."""
 import os
 import shutil
 import subprocess

@@ -253,3 +253,78 @@ def emulate(n, C, seed):
 def test_schedule_is_complete_deadlock_free_and_solves(n, C):
     for seed in range(4):
         assert emulate(n, C, seed) < 1e-10
+
+
+def emulate_backward(nblk, seed):
+    """The chain CTA's backward solve as the kernel runs it: warp 0 (x_J =
+    v_J - P_J x_{J+1}), warp 9 (v_J = M_J t_J once row J is ready) and six
+    helper warps (helper h owns the rows I = h mod 6 and applies x_K's terms
+    L_KI^T x_K as x_K appears, K descending, row K-2 first, then marks row
+    K-2 ready).  The warps step in random interleavings, each waiting on the
+    counters the kernel waits on, and x must equal the triangular solve."""
+    rng = np.random.default_rng(seed)
+    n = B * nblk
+    Lf = np.tril(rng.standard_normal((n, n)) * 0.3, -1) + np.eye(n)
+    z = rng.standard_normal(n)
+    blk = lambda a, i, j: a[B * i:B * i + B, B * j:B * j + B]
+    Ms = [np.linalg.inv(blk(Lf, J, J)).T for J in range(nblk)]
+    Ps = [Ms[J] @ blk(Lf, J + 1, J).T if J + 1 < nblk else None for J in range(nblk)]
+    t = z.copy()
+    xs = np.full(n, np.nan)
+    cnt = {"x": 0, "v": 0}
+    ready = [False] * nblk
+    H = 6
+
+    def warp0():
+        for J in range(nblk - 1, -1, -1):
+            y = Ps[J] @ xs[B * (J + 1):B * (J + 2)] if J + 1 < nblk else 0.0
+            yield True
+            while cnt["v"] < nblk - J:
+                yield False
+            xs[B * J:B * J + B] = t[B * J:B * J + B] - y
+            cnt["x"] = nblk - J
+            yield True
+
+    def warp9():
+        for J in range(nblk - 1, -1, -1):
+            while J + 2 < nblk and not ready[J]:
+                yield False
+            t[B * J:B * J + B] = Ms[J] @ t[B * J:B * J + B]
+            cnt["v"] = nblk - J
+            yield True
+
+    def helper(h):
+        for K in range(nblk - 1, 1, -1):
+            top = K - 2
+            if top < h:
+                continue
+            while cnt["x"] < nblk - K:
+                yield False
+            x_k = xs[B * K:B * K + B].copy()
+            assert not np.isnan(x_k).any()
+            for I in range(top - (top - h) % H, -1, -H):
+                t[B * I:B * I + B] -= blk(Lf, K, I).T @ x_k
+                if I == top:
+                    ready[I] = True
+                yield True
+
+    agents = [warp0(), warp9()] + [helper(h) for h in range(H)]
+    alive = [True] * len(agents)
+    while any(alive):
+        progress = False
+        for a in rng.permutation(len(agents)):
+            if alive[a]:
+                try:
+                    progress |= next(agents[a])
+                except StopIteration:
+                    alive[a] = False
+                    progress = True
+        assert progress, f"backward solve deadlock at nblk={nblk}"
+    ref = np.linalg.solve(Lf.T, z)
+    return np.abs(xs - ref).max() / np.abs(ref).max()
+
+
+@pytest.mark.parametrize("nblk", [1, 2, 3, 4, 7, 11, 17, 24])
+def test_backward_dataflow_is_deadlock_free_and_solves(nblk):
+    for seed in range(4):
+        assert emulate_backward(nblk, seed) < 1e-9
