@@ -546,13 +546,16 @@ __device__ void chain_cta(const Geo& g, const double* S, double* ws, double* x, 
   //                 t and applies x_K's terms to them as x_K appears (K
   //                 descending; row K-2, needed next, first), then marks
   //                 row K-2 ready
-  //        warp 9:  v_J = M_J t_J into t's row J once row J is ready
+  //        warp 4:  v_J = M_J t_J into t's row J once row J is ready
   //        warp 0:  P_J x_{J+1}, then x_J = v_J - P_J x_{J+1}
+  //      (warps 0 and 4 share sub-partition 0, the helpers two to each of
+  //      the others: so each sub-partition's FP64 pipe carries about the
+  //      same number of products)
   //      The warps hand over through counters in shared memory (release /
   //      acquire at CTA scope): rows of x published, rows of v formed and a
   //      ready mark per row.  Each warp loads the tiles it multiplies by
-  //      (P_J, M_J, L_KI) from L2 straight into registers, two rows (warps
-  //      0 and 9) or one term (helpers) ahead of their use, so no copy into
+  //      (P_J, M_J, L_KI) from L2 straight into registers, two rows or two
+  //      terms ahead of their use, so no copy into
   //      shared memory paces the rows (bulk copies of the rows into shared
   //      memory took ~1.1 us a row to issue and land).  Every producer of
   //      the counters runs inside the CTA whatever the abort word says, so
@@ -585,9 +588,9 @@ __device__ void chain_cta(const Geo& g, const double* S, double* ws, double* x, 
   // three register tiles per warp, in rotation: each load is made two rows
   // (or two terms) ahead of its use and used where it landed
   double b0[8] = {}, b1[8] = {}, b2[8] = {};
-  // warp 0: P_{nblk-2} and P_{nblk-3}; warp 9: M_{nblk-2} and M_{nblk-3}
+  // warp 0: P_{nblk-2} and P_{nblk-3}; warp 4: M_{nblk-2} and M_{nblk-3}
   // (M_{nblk-1} the chain CTA formed in shared memory)
-  if (warp == 0 || warp == 9) {
+  if (warp == 0 || warp == 4) {
     const double* base = warp == 0 ? Pg : Mg;
     if (nblk >= 2) load8(b0, base + (size_t)(nblk - 2) * kTile);
     if (nblk >= 3) load8(b1, base + (size_t)(nblk - 3) * kTile);
@@ -629,7 +632,7 @@ __device__ void chain_cta(const Geo& g, const double* S, double* ws, double* x, 
     row(b2, nblk - 1);
     for (int J = nblk - 2; step(b0, b2, J) && step(b1, b0, J - 1) && step(b2, b1, J - 2); J -= 3) {
     }
-  } else if (warp == 9) {
+  } else if (warp == 4) {
     // v_J = M_J t_J into t's row J once row J is ready
     auto row = [&](const double(&Mr)[8], int J) {
       if (J + 2 < nblk) wait_local(ready + J, 1, abort_word);
@@ -662,8 +665,7 @@ __device__ void chain_cta(const Geo& g, const double* S, double* ws, double* x, 
     }
     for (int J = nblk - 2; step(b0, b2, J) && step(b1, b0, J - 1) && step(b2, b1, J - 2); J -= 3) {
     }
-  } else if (warp != 4 && warp != 8) {
-    // warp 4 shares warp 0's sub-partition and stays out of the FP64 work
+  } else if (warp < 8) {
     const int hw = warp < 4 ? warp - 1 : warp - 2;  // helper 0..5: sub-partitions 1, 2, 3, 1, 2, 3
     // this helper's terms (K, I): K = nblk-1 .. 2, its rows I <= K-2
     // descending; advance to the term after (K, I) (I = -1: none left)

@@ -257,7 +257,7 @@ def test_schedule_is_complete_deadlock_free_and_solves(n, C):
 
 def emulate_backward(nblk, seed):
     """The chain CTA's backward solve as the kernel runs it: warp 0 (x_J =
-    v_J - P_J x_{J+1}), warp 9 (v_J = M_J t_J once row J is ready) and six
+    v_J - P_J x_{J+1}), warp 4 (v_J = M_J t_J once row J is ready) and six
     helper warps (helper h owns the rows I = h mod 6 and applies x_K's terms
     L_KI^T x_K as x_K appears, K descending, row K-2 first, then marks row
     K-2 ready).  The warps step in random interleavings, each waiting on the
@@ -285,7 +285,7 @@ def emulate_backward(nblk, seed):
             cnt["x"] = nblk - J
             yield True
 
-    def warp9():
+    def warp4():
         for J in range(nblk - 1, -1, -1):
             while J + 2 < nblk and not ready[J]:
                 yield False
@@ -308,7 +308,7 @@ def emulate_backward(nblk, seed):
                     ready[I] = True
                 yield True
 
-    agents = [warp0(), warp9()] + [helper(h) for h in range(H)]
+    agents = [warp0(), warp4()] + [helper(h) for h in range(H)]
     alive = [True] * len(agents)
     while any(alive):
         progress = False
