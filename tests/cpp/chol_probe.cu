@@ -1,9 +1,11 @@
 // Test probe for the cluster factorisation: runs k_ldlt_cluster once on a
 // host matrix laid out like the solver's S (row stride ld, identity padding
 // beyond n, right-hand side in row ld) and returns x, the solve flag and the
-// kernel time.  With hold != 0 the workers leave the flag of the first
-// right-hand-side panel unreleased, so the waits on it run out and the solve
-// must report failure instead of hanging.  Built by tests/test_chol_gpu.py.
+// kernel time.  With hold = 1 the workers leave the flag of the first
+// right-hand-side panel unreleased, with hold = 2 the flag of the first
+// backward-solve inverse (M_0, P_0), so the waits on it run out and the
+// solve must report failure instead of hanging.  Built by
+// tests/test_chol_gpu.py.
 #include "mcba_chol.cu"
 
 #include <cuda_runtime.h>
@@ -31,7 +33,8 @@ extern "C" int chol_probe_solve(const double* S_host, int n, int ld, double* x_h
     rc = -6;
   } else {
     Geo g = make_geo(plan.cluster, ld, n);
-    if (hold) g.hold = g.nblk * g.nblk;  // flag of right-hand-side panel (nblk, 0)
+    if (hold == 1) g.hold = g.nblk * g.nblk;  // flag of right-hand-side panel (nblk, 0)
+    if (hold == 2) g.hold = g.inv_index(0);   // flag of the inverse M_0 and product P_0
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(plan.cluster, 1, 1);
     cfg.blockDim = dim3(kThreads, 1, 1);

@@ -75,9 +75,14 @@ def test_indefinite_system_fails_and_leaves_x(probe):
     assert np.all(x == SENTINEL)
 
 
-def test_wait_that_runs_out_ends_in_a_failed_solve(probe):
+@pytest.mark.parametrize("hold", [1, 2], ids=["rhs_panel_flag", "inverse_flag"])
+def test_wait_that_runs_out_ends_in_a_failed_solve(probe, hold):
+    """A flag the workers leave unreleased (the first right-hand-side panel's,
+    or the first backward-solve inverse's): the waits on it give up after
+    their 1 s limit, the solve reports failure, and the context stays
+    usable."""
     A, b = _spd(168, 8)
-    rc, _, ok, ms = _solve(probe, A, b, hold=True)
+    rc, _, ok, ms = _solve(probe, A, b, hold=hold)
     assert rc == 0 and ok == 0
     assert ms < 20000.0
     # the context is still usable: the same system solves normally
