@@ -555,11 +555,11 @@ __device__ void chain_cta(const Geo& g, const double* S, double* ws, double* x, 
   //      acquire at CTA scope): rows of x published, rows of v formed and a
   //      ready mark per row.  Each warp loads the tiles it multiplies by
   //      (P_J, M_J, L_KI) from L2 straight into registers, two rows or two
-  //      terms ahead of their use, so no copy into
-  //      shared memory paces the rows (bulk copies of the rows into shared
-  //      memory took ~1.1 us a row to issue and land).  Every producer of
-  //      the counters runs inside the CTA whatever the abort word says, so
-  //      their waits do not end on it.
+  //      terms ahead of their use, so no copy into shared memory paces the
+  //      rows (bulk copies of the rows into shared memory took ~1.1 us a row
+  //      to issue and land).  Warps 8 and 9 take no part after warp 8's
+  //      waits below.  Every producer of the counters runs inside the CTA
+  //      whatever the abort word says, so their waits do not end on it.
   //      Right-hand-side panel J is done only after every L_JI was (its
   //      updates read them), and the last right-hand-side tile waited above
   //      covers row nblk-1; so warp 8 waits for the right-hand-side panels
